@@ -1,0 +1,175 @@
+/*
+ * sph_c.h - C ABI of the GB300-native WCSPH step (libsph_gb300.so).
+ *
+ * This is the boundary under which NCCA/libfluid's FluidSystem
+ * (libfluid/include/fluidsystem.h:16-126) is replaced.  Every entry point
+ * names the reference member it stands for.  Plain pointers and sizes only:
+ * positions, velocities and colours cross the boundary as packed float32 xyz
+ * triples (the layout of std::vector<float3>), n particles = 3n floats.
+ *
+ * Errors: every function returns SPH_OK (0) or an SPH_E* code; the message
+ * of the last failure on a handle is available from sph_last_error().  The
+ * reference returns void and calls exit(0) on CUDA errors
+ * (fluidparams.cu:222-227, fluidsystem.cu:253-258); this library never exits.
+ *
+ * Threading: a handle is used by one host thread at a time.  Each handle owns
+ * a CUDA stream and its own parameter block in device memory, so any number
+ * of handles coexist (the reference keeps one __constant__ block per process,
+ * fluidparams.cu:6).
+ */
+#ifndef SPH_C_H
+#define SPH_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum sph_status {
+    SPH_OK = 0,
+    SPH_EINVAL = 1,    /* bad argument or call order */
+    SPH_ENOMEM = 2,    /* device allocation failed or budget exceeded */
+    SPH_ECUDA = 3,     /* CUDA runtime error */
+    SPH_ENAN = 4,      /* a non-finite particle position appeared */
+    SPH_ETIMEOUT = 5,  /* a bounded wait ran out */
+    SPH_ENOTINIT = 6,  /* advance/export before init (the reference silently returns) */
+    SPH_ECELL = 7,     /* a grid cell held more particles than supported (8192) */
+    SPH_EBUSY = 8      /* request rejected: over capacity */
+};
+
+typedef struct sph_system sph_system;
+
+/* ---- lifetime ---------------------------------------------------------- */
+/* FluidSystem::FluidSystem (fluidsystem.cu:18-22): parameters take the
+ * FluidParams constructor defaults (fluidparams.cuh:81-97).  device < 0 uses
+ * the current CUDA device. */
+int sph_create(sph_system** out, int device);
+/* FluidSystem::~FluidSystem (fluidsystem.cu:27-31) */
+int sph_destroy(sph_system* s);
+/* FluidSystem::clear (fluidsystem.cu:36-52) */
+int sph_clear(sph_system* s);
+/* FluidSystem::init (fluidsystem.cu:196-265): unit cube, res^3 cells, h=1/res,
+ * parameter resets of fluidsystem.cu:202-235, zeroed state. */
+int sph_init(sph_system* s, uint32_t num_points, uint32_t res);
+/* FluidSystem::setup (fluidsystem.cu:132-147): init + one block [0.1,0.9]^3 */
+int sph_setup(sph_system* s, uint32_t num_points, uint32_t res);
+/* FluidSystem::setupFromData (fluidsystem.cu:179-189): init + copy */
+int sph_setup_from_data(sph_system* s, const float* pos, const float* vel, uint32_t n, uint32_t res);
+/* FluidSystem::createFluidBlock (fluidsystem.cu:66-127), protected in the
+ * reference and used by its subclasses (test/src/myfluidsystem.cpp:14-30). */
+int sph_create_block(sph_system* s, uint32_t first, uint32_t n, float min_x, float min_y, float min_z,
+                     float max_x, float max_y, float max_z);
+/* Overwrite positions (and velocities when vel != NULL) of all particles;
+ * accelerations are zeroed, as after init.  The copy half of setupFromData. */
+int sph_set_state(sph_system* s, const float* pos, const float* vel, uint32_t n);
+
+/* ---- stepping ---------------------------------------------------------- */
+/* FluidSystem::advance (fluidsystem.cu:273-399).  Runs the substeps the
+ * reference's float loop `for (dt = part; dt <= full; dt += part)` would run
+ * (e.g. advance(0.01, 10) runs 9), each with dt = full_dt/substeps.  Blocks
+ * until the work is done.  *executed (may be NULL) receives the count.
+ * A loop that would never terminate in the reference returns SPH_EINVAL. */
+int sph_advance(sph_system* s, float full_dt, uint32_t substeps, uint32_t* executed);
+/* As sph_advance but returns after enqueueing; pair with sph_sync. */
+int sph_advance_async(sph_system* s, float full_dt, uint32_t substeps, uint32_t* executed);
+int sph_sync(sph_system* s);
+/* Substep count of the reference loop, without running it. */
+int64_t sph_substep_count(float full_dt, uint32_t substeps);
+
+/* ---- readback ---------------------------------------------------------- */
+/* FluidSystem::exportToData (fluidsystem.cu:154-173): positions, density
+ * colour (DensityColourOperator, fluidutil.cu:67-80) and velocities in the
+ * order of the last substep's cell sort.  Any pointer may be NULL. */
+int sph_export(sph_system* s, float* pos, float* colour, float* vel, uint32_t n);
+/* FluidSystem::getPscale (fluidsystem.cu:406-409) */
+int sph_get_pscale(const sph_system* s, float* out);
+uint32_t sph_num_particles(const sph_system* s);
+int sph_is_init(const sph_system* s);
+
+/* ---- parameters: FluidSystem setters (fluidsystem.cu:412-475) ---------- */
+int sph_set_rest_density(sph_system* s, float v);   /* setRestDensity */
+int sph_set_particle_size(sph_system* s, float v);  /* setParticleSize */
+int sph_set_gas_constant(sph_system* s, float v);   /* setGasConstant */
+int sph_set_limits(sph_system* s, float vel_limit, float acc_limit); /* setLimits */
+int sph_set_xsph_scale(sph_system* s, float v);     /* setXSPHScale */
+int sph_set_surface_tension(sph_system* s, float v);/* setSurfaceTension */
+int sph_set_viscosity(sph_system* s, float v);      /* setViscosity */
+int sph_set_adhesion(sph_system* s, float v);       /* setAdhesion */
+int sph_set_vdamp(sph_system* s, float v);          /* setVDamp */
+int sph_set_gamma(sph_system* s, float v);          /* setGamma */
+int sph_set_mass(sph_system* s, float v);           /* setMass */
+/* Additions (no reference setter): gravity is fixed at (0,-9.8,0) in the
+ * reference (fluidparams.cuh:97); the domain is the unit cube (fluidutil.cu:85-102). */
+int sph_set_gravity(sph_system* s, float gx, float gy, float gz);
+/* Rectangular box [0,lx]x[0,ly]x[0,lz] with cell size h (the smoothing
+ * length).  Reallocates the grid; particle state is kept. */
+int sph_set_domain(sph_system* s, float lx, float ly, float lz, float h);
+
+/* Whole parameter set, for inspection and bulk configuration. */
+typedef struct sph_params {
+    uint32_t box_mode;   /* 0: unit cube with res cells per axis; 1: box lx,ly,lz with cell h */
+    uint32_t res;
+    float lx, ly, lz, h;
+    float rest_density, gas_constant, gamma, mass, particle_size;
+    float xsph, surface_tension, viscosity, adhesion, vdamp;
+    float vel_limit, acc_limit, dt;
+    float gravity[3];
+} sph_params;
+int sph_get_params(const sph_system* s, sph_params* out);
+int sph_set_params(sph_system* s, const sph_params* p);
+
+/* Derived device parameter block as doubles, in this order: gx, gy, gz,
+ * inv_cell, h, h2, poly6, grad_poly6, grad_spiky, cohesion, invh9,
+ * rest_density, gas_constant, gamma, mass, particle_size, dt, xsph,
+ * surface_tension, viscosity, adhesion, vdamp, vel_limit, acc_limit,
+ * gravity xyz, eps.  Returns the number written. */
+int sph_get_derived(const sph_system* s, double* out, int cap);
+
+/* ---- parity / debug taps ----------------------------------------------- */
+/* Per-particle and per-cell intermediates of the last substep, indexed like
+ * the reference's device vectors after that substep (cell order). */
+enum sph_field {
+    SPH_FIELD_HASH = 0,       /* u32[n]  m_Hash after the sort (NULL_HASH = 0xFFFFFFFF) */
+    SPH_FIELD_PERM = 1,       /* u32[n]  pre-sort index of the particle now at each slot */
+    SPH_FIELD_CELLSTART = 2,  /* u32[cells] m_ScatterAddress */
+    SPH_FIELD_CELLOCC = 3,    /* u32[cells] m_CellOcc */
+    SPH_FIELD_NBRCOUNT = 4,   /* u32[n]  neighbours j != i with r^2 <= h^2 (needs debug taps) */
+    SPH_FIELD_DENSITY = 5,    /* f32[n]  m_Density */
+    SPH_FIELD_PRESSURE = 6,   /* f32[n]  m_Pressure */
+    SPH_FIELD_SOUNDSPEED = 7, /* f32[n]  m_SoundSpeed */
+    SPH_FIELD_FPRESSURE = 8,  /* f32[3n] pressure force (needs debug taps) */
+    SPH_FIELD_FTENSION = 9,   /* f32[3n] tension force (needs debug taps) */
+    SPH_FIELD_FADHESION = 10, /* f32[3n] adhesion force (needs debug taps) */
+    SPH_FIELD_FVISCOSITY = 11,/* f32[3n] viscosity force (needs debug taps) */
+    SPH_FIELD_NORMAL = 12,    /* f32[3n] m_Normals (surface tension scenes only) */
+    SPH_FIELD_POS_SORTED = 13,/* f32[3n] positions in cell order before integration */
+    SPH_FIELD_ACC = 14        /* f32[3n] m_Acceleration */
+};
+/* Enable the optional taps (neighbour counts, force components). */
+int sph_debug_enable(sph_system* s, int on);
+int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
+
+/* ---- execution options and profiling ----------------------------------- */
+int sph_set_use_graph(sph_system* s, int on);     /* CUDA-graph replay of the substep (default on) */
+int sph_set_profiling(sph_system* s, int on);     /* per-pass CUDA events (disables the graph) */
+/* Accumulated per-pass milliseconds since profiling was enabled, in the
+ * order hash, scan, sort, density, normals, force_integrate, xsph, substep. */
+int sph_get_pass_times(sph_system* s, double* ms, int cap, uint64_t* substeps);
+const char* sph_pass_name(int i);
+/* Page-lock (or release) a caller's host buffer so transfers to and from
+ * it run at full link speed (cudaHostRegister). */
+int sph_host_register(void* ptr, uint64_t bytes);
+int sph_host_unregister(void* ptr);
+/* Device timing on the handle's stream: record CUDA event `slot` (0..63);
+ * elapsed milliseconds between two recorded slots (waits for slot b). */
+int sph_timer_mark(sph_system* s, int slot);
+int sph_timer_elapsed(sph_system* s, int a, int b, float* ms);
+const char* sph_last_error(const sph_system* s);
+const char* sph_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPH_C_H */

@@ -1,0 +1,690 @@
+// Host-side engine (see engine.h).
+#include "engine.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+namespace sph {
+
+namespace {
+constexpr float PI_F = 3.141592654f;   // fluiddefines.h:16 (CUDART_PI_F)
+const char* kPassNames[Engine::kPasses] = {"hash", "scan", "sort", "density", "normals", "force_integrate",
+                                           "xsph", "substep"};
+}  // namespace
+
+bool derive_params(const SceneConfig& c, DevParams& d, std::string* err) {
+    std::memset(&d, 0, sizeof(d));
+    float h;
+    if (c.box_mode == 0) {
+        if (c.res == 0) { if (err) *err = "res must be positive"; return false; }
+        d.gx = d.gy = d.gz = c.res;
+        d.inv_cell = float(c.res);                      // grid_from_point multiplies by m_res (fluidutil.cu:17)
+        d.box_cx = d.box_cy = d.box_cz = 0.5f;          // unit cube SDF (fluidutil.cu:87)
+        d.box_bx = d.box_by = d.box_bz = 0.5f;
+        h = 1.0f / float(c.res);                        // fluidparams.cu:62
+    } else {
+        if (!(c.h > 0.f) || !(c.lx > 0.f) || !(c.ly > 0.f) || !(c.lz > 0.f)) {
+            if (err) *err = "box extents and h must be positive";
+            return false;
+        }
+        // cells per axis: ceil(l/h), tolerant to the float rounding of h
+        auto cells = [&](float l) -> uint32_t {
+            const double v = std::ceil(double(l) / double(c.h) - 1e-3);
+            return v < 1.0 ? 1u : (uint32_t)v;
+        };
+        d.gx = cells(c.lx); d.gy = cells(c.ly); d.gz = cells(c.lz);
+        d.inv_cell = 1.0f / c.h;
+        d.box_cx = d.box_bx = 0.5f * c.lx;
+        d.box_cy = d.box_by = 0.5f * c.ly;
+        d.box_cz = d.box_bz = 0.5f * c.lz;
+        h = c.h;
+    }
+    const uint64_t cells = (uint64_t)d.gx * d.gy * d.gz;
+    if (cells >= (1ull << 31)) { if (err) *err = "grid too large"; return false; }
+    d.gxy = d.gx * d.gy;
+    d.ncells = (uint32_t)cells;
+    // fluidparams.cu:63-86
+    d.h = h;
+    d.halfh = 0.5f * h;
+    d.h2 = h * h;
+    const float h3 = h * h * h;
+    d.h4 = h * h * h * h;
+    const float h5 = h3 * d.h2;
+    d.h6 = h3 * h3;
+    d.h8 = h5 * h3;
+    d.h9 = d.h6 * h3;
+    d.invh9 = 1.0f / (d.h6 * h3);
+    d.poly6 = 315.0f / (64.0f * PI_F * powf(h, 9.0f));
+    d.grad_poly6 = -945.0f / (32.0f * PI_F * powf(h, 9.0f));
+    d.grad_spiky = -45.0f / (PI_F * powf(h, 6.0f));
+    d.cohesion = 32.0f / (PI_F * powf(h, 9.0f));
+    d.visc_eps = (float)(0.01 * (double)d.h2);
+    // fluid parameters (fluidparams.cu:99-213)
+    d.rest_density = c.rest_density;
+    d.inv_rest_density = (c.rest_density == 0.0f) ? 1.0f : 1.0f / c.rest_density;
+    d.gas_constant = c.gas_constant;
+    d.gamma = c.gamma;
+    const float inv_gamma = (c.gamma == 0.0f) ? 1.0f : 1.0f / c.gamma;
+    d.eos_k = c.gas_constant * c.rest_density * inv_gamma;
+    d.mass = c.mass;
+    d.two_mass = 2.0f * c.mass;
+    d.particle_size = c.particle_size;
+    d.inv_particle_size = 1.0f / c.particle_size;
+    d.dt = c.dt;
+    d.dtdt = c.dt * c.dt;
+    d.xsph = c.xsph;
+    d.surface_tension = c.surface_tension;
+    d.viscosity = c.viscosity;
+    d.adhesion = c.adhesion;
+    d.vdamp = c.vdamp;
+    d.vel_limit = c.vel_limit;
+    d.acc_limit = c.acc_limit;
+    d.vel_limit2 = c.vel_limit * c.vel_limit;
+    d.acc_limit2 = c.acc_limit * c.acc_limit;
+    d.grav_x = c.gravity[0]; d.grav_y = c.gravity[1]; d.grav_z = c.gravity[2];
+    d.eps = FLT_MIN;
+    d.flags = (c.surface_tension != 0.0f) ? 1u : 0u;
+    return true;
+}
+
+uint64_t Engine::bytes_per_particle() { return 9 * 16 + 4 * 4; }
+uint64_t Engine::bytes_per_cell() { return 2 * 4 + 1; }
+const char* Engine::pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : "?"; }
+
+Engine::Engine(int device) {
+    if (device < 0) cudaGetDevice(&device_);
+    else device_ = device;
+    cudaSetDevice(device_);
+    cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
+    cudaMallocHost((void**)&h_status_, sizeof(uint32_t));
+    cudaMalloc((void**)&status_, sizeof(uint32_t));
+    cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_);
+    for (auto& e : ev_) cudaEventCreate(&e);
+}
+
+Engine::~Engine() {
+    cudaSetDevice(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    free_all();
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    for (auto& e : ev_) if (e) cudaEventDestroy(e);
+    for (auto& e : timers_) if (e) cudaEventDestroy(e);
+    if (status_) cudaFree(status_);
+    if (h_status_) cudaFreeHost(h_status_);
+    if (h_params_) cudaFreeHost(h_params_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Engine::fail(int code, const std::string& msg) {
+    err_ = msg;
+    return code;
+}
+int Engine::cuda_fail(cudaError_t e, const char* what) {
+    err_ = std::string(what) + ": " + cudaGetErrorString(e);
+    return ENG_ECUDA;
+}
+#define ENG_CK(expr, what)                       \
+    do {                                         \
+        cudaError_t e__ = (expr);                \
+        if (e__ != cudaSuccess) return cuda_fail(e__, what); \
+    } while (0)
+
+void Engine::free_all() {
+    float4** f4[] = {&P0_, &P1_, &V0_, &V1_, &V2_, &A0_, &A1_, &S_, &N_, &dbg_forces_};
+    for (auto p : f4) { if (*p) cudaFree(*p); *p = nullptr; }
+    uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &count_, &start_, &scan_sums_, &dbg_nbr_};
+    for (auto p : u) { if (*p) cudaFree(*p); *p = nullptr; }
+    if (stage_) cudaFree(stage_);
+    stage_ = nullptr;
+    stage_bytes_ = 0;
+    if (d_params_) cudaFree(d_params_);
+    if (d_scenes_) cudaFree(d_scenes_);
+    if (d_tiles_) cudaFree(d_tiles_);
+    d_params_ = nullptr; d_scenes_ = nullptr; d_tiles_ = nullptr;
+    pcap_ = ccap_ = 0;
+    dev_bytes_ = 0;
+}
+
+// Grow the particle and cell arenas, preserving live particle state.
+int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
+    cudaSetDevice(device_);
+    if (parts > pcap_) {
+        const uint64_t np = std::max<uint64_t>(parts, pcap_ + pcap_ / 2);
+        if (np >= (1ull << 31)) return fail(ENG_ENOMEM, "particle capacity exceeds 2^31");
+        float4** state[] = {&P0_, &V0_, &A0_, &S_};
+        float4** scratch[] = {&P1_, &V1_, &V2_, &A1_, &N_};
+        for (auto p : state) {
+            float4* q = nullptr;
+            cudaError_t e = cudaMalloc((void**)&q, np * sizeof(float4));
+            if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+            if (*p) {
+                ENG_CK(cudaMemcpyAsync(q, *p, pcap_ * sizeof(float4), cudaMemcpyDeviceToDevice, stream_), "grow copy");
+                ENG_CK(cudaStreamSynchronize(stream_), "grow sync");
+                cudaFree(*p);
+            }
+            *p = q;
+        }
+        for (auto p : scratch) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+            cudaError_t e = cudaMalloc((void**)p, np * sizeof(float4));
+            if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+        }
+        uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_};
+        for (auto p : u) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+            cudaError_t e = cudaMalloc((void**)p, np * sizeof(uint32_t));
+            if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+        }
+        if (dbg_nbr_) { cudaFree(dbg_nbr_); dbg_nbr_ = nullptr; }
+        if (dbg_forces_) { cudaFree(dbg_forces_); dbg_forces_ = nullptr; }
+        if (debug_) {
+            ENG_CK(cudaMalloc((void**)&dbg_nbr_, np * sizeof(uint32_t)), "debug alloc");
+            ENG_CK(cudaMalloc((void**)&dbg_forces_, np * 4 * sizeof(float4)), "debug alloc");
+        }
+        pcap_ = np;
+        graph_dirty_ = true;
+    }
+    if (cells > ccap_) {
+        const uint64_t nc = std::max<uint64_t>(cells, ccap_ + ccap_ / 2);
+        if (count_) cudaFree(count_);
+        if (start_) cudaFree(start_);
+        if (scan_sums_) cudaFree(scan_sums_);
+        count_ = start_ = scan_sums_ = nullptr;
+        cudaError_t e1 = cudaMalloc((void**)&count_, nc * sizeof(uint32_t));
+        cudaError_t e2 = cudaMalloc((void**)&start_, (nc + 1) * sizeof(uint32_t));
+        cudaError_t e3 = cudaMalloc((void**)&scan_sums_, (nc / 4096 + 2) * sizeof(uint32_t));
+        if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
+            return fail(ENG_ENOMEM, "device allocation of cell arrays failed");
+        ccap_ = nc;
+        graph_dirty_ = true;
+    }
+    dev_bytes_ = pcap_ * bytes_per_particle() + ccap_ * 8;
+    return ENG_OK;
+}
+
+uint32_t Engine::alloc_slots(uint32_t n) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+        if (it->second >= n) {
+            const uint32_t base = it->first;
+            const uint32_t rest = it->second - n;
+            free_.erase(it);
+            if (rest) free_[base + n] = rest;
+            return base;
+        }
+    }
+    const uint32_t base = (uint32_t)slots_end_;
+    slots_end_ += n;
+    return base;
+}
+
+void Engine::free_slots(uint32_t base, uint32_t n) {
+    if (n == 0) return;
+    if ((uint64_t)base + n == slots_end_) {
+        slots_end_ = base;
+        // merge a trailing free range
+        while (!free_.empty()) {
+            auto last = std::prev(free_.end());
+            if ((uint64_t)last->first + last->second == slots_end_) {
+                slots_end_ = last->first;
+                free_.erase(last);
+            } else break;
+        }
+        return;
+    }
+    auto it = free_.emplace(base, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+    if (it != free_.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+    }
+}
+
+int Engine::staging(size_t bytes, float** out) {
+    if (bytes > stage_bytes_) {
+        if (stage_) { cudaStreamSynchronize(stream_); cudaFree(stage_); }
+        stage_ = nullptr;
+        stage_bytes_ = 0;
+        ENG_CK(cudaMalloc((void**)&stage_, bytes), "staging alloc");
+        stage_bytes_ = bytes;
+    }
+    *out = stage_;
+    return ENG_OK;
+}
+
+uint64_t Engine::total_particles() const {
+    uint64_t t = 0;
+    for (const auto& s : scenes_) t += s.n;
+    return t;
+}
+
+const Scene* Engine::scene(int id) const {
+    for (const auto& s : scenes_) if (s.id == id) return &s;
+    return nullptr;
+}
+
+int Engine::add_scene(const SceneConfig& cfg, uint32_t n, int* id_out) {
+    Scene s;
+    std::string e;
+    if (!derive_params(cfg, s.dp, &e)) return fail(ENG_EINVAL, e);
+    if (n == 0) return fail(ENG_EINVAL, "a scene needs at least one particle");
+    s.cfg = cfg;
+    s.n = n;
+    s.id = next_id_++;
+    s.part_base = alloc_slots(n);
+    uint64_t cells = 0;
+    for (const auto& t : scenes_) cells += t.dp.ncells + 1ull;
+    cells += s.dp.ncells + 1ull;
+    int rc = ensure_capacity(slots_end_, cells);
+    if (rc) { free_slots(s.part_base, n); return rc; }
+    scenes_.push_back(s);
+    layout_dirty_ = params_dirty_ = true;
+    if (id_out) *id_out = s.id;
+    return ENG_OK;
+}
+
+int Engine::remove_scene(int id) {
+    for (size_t k = 0; k < scenes_.size(); ++k) {
+        if (scenes_[k].id == id) {
+            free_slots(scenes_[k].part_base, scenes_[k].n);
+            scenes_.erase(scenes_.begin() + k);
+            layout_dirty_ = params_dirty_ = true;
+            return ENG_OK;
+        }
+    }
+    return fail(ENG_EINVAL, "unknown scene id");
+}
+
+int Engine::set_config(int id, const SceneConfig& cfg) {
+    for (auto& s : scenes_) {
+        if (s.id != id) continue;
+        DevParams dp;
+        std::string e;
+        if (!derive_params(cfg, dp, &e)) return fail(ENG_EINVAL, e);
+        if (dp.ncells != s.dp.ncells || dp.flags != s.dp.flags) layout_dirty_ = true;
+        s.cfg = cfg;
+        if (std::memcmp(&dp, &s.dp, sizeof(DevParams)) != 0) params_dirty_ = true;
+        s.dp = dp;
+        if (layout_dirty_) {
+            uint64_t cells = 0;
+            for (const auto& t : scenes_) cells += t.dp.ncells + 1ull;
+            int rc = ensure_capacity(slots_end_, cells);
+            if (rc) return rc;
+        }
+        return ENG_OK;
+    }
+    return fail(ENG_EINVAL, "unknown scene id");
+}
+
+int Engine::rebuild_layout() {
+    cudaSetDevice(device_);
+    const size_t ns = scenes_.size();
+    h_scenes_.resize(ns);
+    h_tiles_.clear();
+    cell_base_.resize(ns);
+    uint64_t cb = 0;
+    any_tension_ = false;
+    for (size_t k = 0; k < ns; ++k) {
+        const Scene& s = scenes_[k];
+        cell_base_[k] = (uint32_t)cb;
+        h_scenes_[k] = DevScene{s.part_base, s.n, (uint32_t)cb, s.dp.ncells};
+        cb += s.dp.ncells + 1ull;
+        for (uint32_t f = 0; f < s.n; f += SPH_TILE)
+            h_tiles_.push_back(make_uint4((uint32_t)k, s.part_base + f, std::min<uint32_t>(SPH_TILE, s.n - f), 0u));
+        any_tension_ = any_tension_ || (s.dp.flags & 1u);
+    }
+    total_cells_ = (uint32_t)cb;
+    int rc = ensure_capacity(slots_end_, cb);
+    if (rc) return rc;
+    if (ns > scene_cap_) {
+        if (d_scenes_) cudaFree(d_scenes_);
+        if (d_params_) cudaFree(d_params_);
+        if (h_params_) cudaFreeHost(h_params_);
+        scene_cap_ = std::max<uint64_t>(ns, scene_cap_ * 2);
+        ENG_CK(cudaMalloc((void**)&d_scenes_, scene_cap_ * sizeof(DevScene)), "scene table");
+        ENG_CK(cudaMalloc((void**)&d_params_, scene_cap_ * sizeof(DevParams)), "param table");
+        ENG_CK(cudaMallocHost((void**)&h_params_, scene_cap_ * sizeof(DevParams)), "param staging");
+        graph_dirty_ = true;
+    }
+    if (h_tiles_.size() > tile_cap_) {
+        if (d_tiles_) cudaFree(d_tiles_);
+        tile_cap_ = std::max<uint64_t>(h_tiles_.size(), tile_cap_ * 2);
+        ENG_CK(cudaMalloc((void**)&d_tiles_, tile_cap_ * sizeof(uint4)), "tile table");
+        graph_dirty_ = true;
+    }
+    if (ns) ENG_CK(cudaMemcpyAsync(d_scenes_, h_scenes_.data(), ns * sizeof(DevScene), cudaMemcpyHostToDevice, stream_), "scene upload");
+    if (!h_tiles_.empty())
+        ENG_CK(cudaMemcpyAsync(d_tiles_, h_tiles_.data(), h_tiles_.size() * sizeof(uint4), cudaMemcpyHostToDevice, stream_), "tile upload");
+    ENG_CK(cudaStreamSynchronize(stream_), "layout sync");
+    layout_dirty_ = false;
+    params_dirty_ = true;
+    graph_dirty_ = true;
+    return ENG_OK;
+}
+
+int Engine::upload_params() {
+    const size_t ns = scenes_.size();
+    // The pinned staging buffer is reused: wait until the previous copy drained.
+    ENG_CK(cudaStreamSynchronize(stream_), "param sync");
+    for (size_t k = 0; k < ns; ++k) h_params_[k] = scenes_[k].dp;
+    if (ns) ENG_CK(cudaMemcpyAsync(d_params_, h_params_, ns * sizeof(DevParams), cudaMemcpyHostToDevice, stream_), "param upload");
+    params_dirty_ = false;
+    return ENG_OK;
+}
+
+StepArgs Engine::args() const {
+    StepArgs a;
+    a.params = d_params_;
+    a.scenes = d_scenes_;
+    a.tiles = d_tiles_;
+    a.ntiles = (uint32_t)h_tiles_.size();
+    a.total_cells = total_cells_;
+    a.P0 = P0_; a.V0 = V0_; a.A0 = A0_;
+    a.P1 = P1_; a.V1 = V1_; a.A1 = A1_;
+    a.V2 = V2_; a.S = S_; a.N = N_;
+    a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
+    a.key = key_; a.slot = slot_; a.tmp = tmp_; a.perm = perm_;
+    a.status = status_;
+    a.dbg_nbr = debug_ ? dbg_nbr_ : nullptr;
+    a.dbg_forces = debug_ ? dbg_forces_ : nullptr;
+    return a;
+}
+
+// Record (or launch) one substep on the stream.
+int Engine::launch_substep(bool profile) {
+    const StepArgs a = args();
+    cudaStream_t st = stream_;
+    auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
+    mark(0);
+    ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), st), "memset counts");
+    ENG_CK(launch_hash(a, st), "hash");
+    mark(1);
+    ENG_CK(launch_scan(a, st), "scan");
+    mark(2);
+    ENG_CK(launch_sort(a, st), "sort");
+    mark(3);
+    ENG_CK(launch_density(a, st), "density");
+    mark(4);
+    if (any_tension_) ENG_CK(launch_normals(a, st), "normals");
+    mark(5);
+    ENG_CK(launch_force(a, st), "force");
+    mark(6);
+    ENG_CK(launch_xsph(a, st), "xsph");
+    mark(7);
+    return ENG_OK;
+}
+
+int Engine::read_status() {
+    ENG_CK(cudaMemcpyAsync(h_status_, status_, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "status read");
+    ENG_CK(cudaStreamSynchronize(stream_), "step sync");
+    const uint32_t st = *h_status_;
+    if (st) {
+        ENG_CK(cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_), "status reset");
+        if (st & SPH_STATUS_CELL_OVERFLOW)
+            return fail(ENG_ECELL, "a grid cell held more than 8192 particles");
+        if (st & SPH_STATUS_NONFINITE) return fail(ENG_ENAN, "non-finite particle position");
+    }
+    return ENG_OK;
+}
+
+int Engine::step(uint32_t substeps, bool sync) {
+    cudaSetDevice(device_);
+    if (scenes_.empty()) return ENG_OK;
+    if (layout_dirty_) { int rc = rebuild_layout(); if (rc) return rc; }
+    if (params_dirty_) { int rc = upload_params(); if (rc) return rc; }
+    const bool graph = use_graph_ && !profiling_;
+    if (graph && (graph_dirty_ || !graph_exec_)) {
+        if (graph_exec_) { cudaGraphExecDestroy(graph_exec_); graph_exec_ = nullptr; }
+        if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+        ENG_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+        int rc = launch_substep(false);
+        cudaGraph_t g = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        ENG_CK(ce, "end capture");
+        graph_ = g;
+        ENG_CK(cudaGraphInstantiate(&graph_exec_, graph_, 0), "graph instantiate");
+        graph_dirty_ = false;
+    }
+    for (uint32_t s = 0; s < substeps; ++s) {
+        if (graph) {
+            ENG_CK(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
+        } else if (profiling_) {
+            int rc = launch_substep(true);
+            if (rc) return rc;
+            ENG_CK(cudaEventSynchronize(ev_[7]), "profile sync");
+            for (int i = 0; i < 7; ++i) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, ev_[i], ev_[i + 1]);
+                // pass i spans events i..i+1, except that pass 0 includes the memset
+                pass_ms_[i] += ms;
+            }
+            float tot = 0.f;
+            cudaEventElapsedTime(&tot, ev_[0], ev_[7]);
+            pass_ms_[7] += tot;
+            prof_substeps_++;
+        } else {
+            int rc = launch_substep(false);
+            if (rc) return rc;
+        }
+    }
+    stepped_ = true;
+    if (sync) return read_status();
+    return ENG_OK;
+}
+
+int Engine::sync() {
+    cudaSetDevice(device_);
+    return read_status();
+}
+
+int Engine::set_profiling(bool on) {
+    profiling_ = on;
+    for (double& v : pass_ms_) v = 0.0;
+    prof_substeps_ = 0;
+    return ENG_OK;
+}
+
+int Engine::timer_mark(int slot) {
+    if (slot < 0 || slot >= 64) return fail(ENG_EINVAL, "timer slot out of range");
+    cudaSetDevice(device_);
+    if (!timers_[slot]) ENG_CK(cudaEventCreate(&timers_[slot]), "timer create");
+    ENG_CK(cudaEventRecord(timers_[slot], stream_), "timer record");
+    return ENG_OK;
+}
+
+int Engine::timer_elapsed(int a, int b, float* ms) {
+    if (a < 0 || a >= 64 || b < 0 || b >= 64 || !timers_[a] || !timers_[b] || !ms)
+        return fail(ENG_EINVAL, "timer slot not recorded");
+    ENG_CK(cudaEventSynchronize(timers_[b]), "timer sync");
+    ENG_CK(cudaEventElapsedTime(ms, timers_[a], timers_[b]), "timer elapsed");
+    return ENG_OK;
+}
+
+int Engine::get_pass_times(double* ms_out, int cap, uint64_t* launches) {
+    for (int i = 0; i < kPasses && i < cap; ++i) ms_out[i] = pass_ms_[i];
+    if (launches) *launches = prof_substeps_;
+    return ENG_OK;
+}
+
+int Engine::set_state(int id, const float* pos, const float* vel, uint32_t n, bool from_device) {
+    cudaSetDevice(device_);
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
+    const float* dpos = pos;
+    const float* dvel = vel;
+    if (!from_device) {
+        const size_t bytes = (size_t)n * 3 * sizeof(float);
+        float* st = nullptr;
+        int rc = staging(2 * bytes, &st);
+        if (rc) return rc;
+        ENG_CK(cudaMemcpyAsync(st, pos, bytes, cudaMemcpyHostToDevice, stream_), "state upload");
+        dpos = st;
+        dvel = nullptr;
+        if (vel) {
+            ENG_CK(cudaMemcpyAsync(st + (size_t)n * 3, vel, bytes, cudaMemcpyHostToDevice, stream_), "state upload");
+            dvel = st + (size_t)n * 3;
+        }
+    }
+    ENG_CK(launch_unpack(dpos, dvel, n, s->part_base, P0_, V0_, A0_, S_, stream_), "unpack");
+    ENG_CK(cudaStreamSynchronize(stream_), "upload sync");
+    return ENG_OK;
+}
+
+int Engine::set_positions(int id, uint32_t first, const float* pos, uint32_t count) {
+    cudaSetDevice(device_);
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    if ((uint64_t)first + count > s->n) return fail(ENG_EINVAL, "range exceeds the scene's particle count");
+    if (count == 0) return ENG_OK;
+    const size_t bytes = (size_t)count * 3 * sizeof(float);
+    float* st = nullptr;
+    int rc = staging(bytes, &st);
+    if (rc) return rc;
+    ENG_CK(cudaMemcpyAsync(st, pos, bytes, cudaMemcpyHostToDevice, stream_), "position upload");
+    ENG_CK(launch_set_positions(st, count, s->part_base + first, P0_, stream_), "set positions");
+    ENG_CK(cudaStreamSynchronize(stream_), "upload sync");
+    return ENG_OK;
+}
+
+int Engine::generate_lattice(int id, const LatticeSpec& spec, uint32_t first) {
+    cudaSetDevice(device_);
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    const uint64_t n = (uint64_t)spec.nx * spec.ny * spec.nz;
+    if (first + n > s->n) return fail(ENG_EINVAL, "lattice exceeds the scene's particle count");
+    ENG_CK(launch_lattice(spec, s->part_base + first, P0_, V0_, A0_, S_, stream_), "lattice");
+    return ENG_OK;
+}
+
+int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n, bool to_device) {
+    cudaSetDevice(device_);
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
+    if (to_device) {
+        ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, pos, colour, vel, stream_), "pack");
+        ENG_CK(cudaStreamSynchronize(stream_), "pack sync");
+        return ENG_OK;
+    }
+    const size_t bytes = (size_t)n * 3 * sizeof(float);
+    float* st = nullptr;
+    int rc = staging(3 * bytes, &st);
+    if (rc) return rc;
+    float* dp = pos ? st : nullptr;
+    float* dc = colour ? st + (size_t)n * 3 : nullptr;
+    float* dv = vel ? st + (size_t)n * 6 : nullptr;
+    ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, dv, stream_), "pack");
+    if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+    if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+    if (vel) ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+    ENG_CK(cudaStreamSynchronize(stream_), "download sync");
+    return ENG_OK;
+}
+
+int Engine::debug_enable(bool on) {
+    if (on == debug_) return ENG_OK;
+    debug_ = on;
+    graph_dirty_ = true;
+    if (on && pcap_) {
+        ENG_CK(cudaMalloc((void**)&dbg_nbr_, pcap_ * sizeof(uint32_t)), "debug alloc");
+        ENG_CK(cudaMalloc((void**)&dbg_forces_, pcap_ * 4 * sizeof(float4)), "debug alloc");
+    }
+    return ENG_OK;
+}
+
+int Engine::debug_get(int id, int field, void* host, uint64_t count) {
+    cudaSetDevice(device_);
+    ENG_CK(cudaStreamSynchronize(stream_), "debug sync");
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    if (!stepped_) return fail(ENG_EINVAL, "no substep has run yet");
+    size_t k = 0;
+    for (; k < scenes_.size(); ++k) if (scenes_[k].id == id) break;
+    const uint32_t n = s->n, nc = s->dp.ncells, cb = cell_base_[k], pb = s->part_base;
+    auto need = [&](uint64_t c) { return count >= c; };
+    switch (field) {
+        case F_HASH: {
+            if (!need(n)) return fail(ENG_EINVAL, "buffer too small");
+            uint32_t* tmp = nullptr;
+            ENG_CK(cudaMalloc((void**)&tmp, n * sizeof(uint32_t)), "debug alloc");
+            ENG_CK(launch_sorted_keys(key_ + 0, perm_, n, pb, nc, tmp, stream_), "sorted keys");
+            // keys are indexed by global slot; launch_sorted_keys reads key[perm[base+i]]
+            ENG_CK(cudaMemcpyAsync(host, tmp, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "debug copy");
+            ENG_CK(cudaStreamSynchronize(stream_), "debug sync");
+            cudaFree(tmp);
+            return ENG_OK;
+        }
+        case F_PERM: {
+            if (!need(n)) return fail(ENG_EINVAL, "buffer too small");
+            uint32_t* out = (uint32_t*)host;
+            ENG_CK(cudaMemcpy(out, perm_ + pb, n * sizeof(uint32_t), cudaMemcpyDeviceToHost), "debug copy");
+            for (uint32_t i = 0; i < n; ++i) out[i] -= pb;
+            return ENG_OK;
+        }
+        case F_CELLSTART:
+        case F_CELLOCC: {
+            if (!need(nc)) return fail(ENG_EINVAL, "buffer too small");
+            std::vector<uint32_t> st(nc + 1);
+            ENG_CK(cudaMemcpy(st.data(), start_ + cb, (nc + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost), "debug copy");
+            uint32_t* out = (uint32_t*)host;
+            for (uint32_t c = 0; c < nc; ++c) out[c] = (field == F_CELLSTART) ? st[c] - st[0] : st[c + 1] - st[c];
+            return ENG_OK;
+        }
+        case F_NBRCOUNT: {
+            if (!debug_ || !dbg_nbr_) return fail(ENG_EINVAL, "debug taps are not enabled");
+            if (!need(n)) return fail(ENG_EINVAL, "buffer too small");
+            ENG_CK(cudaMemcpy(host, dbg_nbr_ + pb, n * sizeof(uint32_t), cudaMemcpyDeviceToHost), "debug copy");
+            return ENG_OK;
+        }
+        case F_DENSITY:
+        case F_PRESSURE:
+        case F_SOUNDSPEED: {
+            if (!need(n)) return fail(ENG_EINVAL, "buffer too small");
+            std::vector<float4> v(n);
+            ENG_CK(cudaMemcpy(v.data(), S_ + pb, n * sizeof(float4), cudaMemcpyDeviceToHost), "debug copy");
+            float* out = (float*)host;
+            for (uint32_t i = 0; i < n; ++i)
+                out[i] = field == F_DENSITY ? v[i].x : field == F_PRESSURE ? v[i].y : v[i].z;
+            return ENG_OK;
+        }
+        case F_FPRESSURE:
+        case F_FTENSION:
+        case F_FADHESION:
+        case F_FVISCOSITY: {
+            if (!debug_ || !dbg_forces_) return fail(ENG_EINVAL, "debug taps are not enabled");
+            if (!need(3ull * n)) return fail(ENG_EINVAL, "buffer too small");
+            std::vector<float4> v((size_t)n * 4);
+            ENG_CK(cudaMemcpy(v.data(), dbg_forces_ + 4 * (size_t)pb, (size_t)n * 4 * sizeof(float4), cudaMemcpyDeviceToHost), "debug copy");
+            const int c = field - F_FPRESSURE;
+            float* out = (float*)host;
+            for (uint32_t i = 0; i < n; ++i) {
+                const float4 f = v[4 * (size_t)i + c];
+                out[3 * i] = f.x; out[3 * i + 1] = f.y; out[3 * i + 2] = f.z;
+            }
+            return ENG_OK;
+        }
+        case F_NORMAL:
+        case F_POS_SORTED:
+        case F_ACC: {
+            if (!need(3ull * n)) return fail(ENG_EINVAL, "buffer too small");
+            const float4* src = field == F_NORMAL ? N_ : field == F_POS_SORTED ? P1_ : A0_;
+            std::vector<float4> v(n);
+            ENG_CK(cudaMemcpy(v.data(), src + pb, n * sizeof(float4), cudaMemcpyDeviceToHost), "debug copy");
+            float* out = (float*)host;
+            for (uint32_t i = 0; i < n; ++i) { out[3 * i] = v[i].x; out[3 * i + 1] = v[i].y; out[3 * i + 2] = v[i].z; }
+            return ENG_OK;
+        }
+        default:
+            return fail(ENG_EINVAL, "unknown debug field");
+    }
+}
+
+}  // namespace sph

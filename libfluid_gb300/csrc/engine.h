@@ -1,0 +1,147 @@
+// Host-side engine: device arenas, scene table, tile list and the captured
+// substep.  One Engine drives any number of independent scenes with one
+// launch per pass; the plain FluidSystem drop-in is an Engine with one scene.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <map>
+#include <string>
+#include <vector>
+#include "sph_types.h"
+#include "sph_kernels.h"
+
+namespace sph {
+
+// User-facing parameters of one scene: the values FluidParams' setters take
+// (fluidparams.cuh:103-117) plus the generalised domain and gravity.
+struct SceneConfig {
+    int box_mode = 0;                 // 0: unit cube with res cells per axis (the reference); 1: box lx,ly,lz, cell h
+    uint32_t res = 1;
+    float lx = 1.f, ly = 1.f, lz = 1.f, h = 1.f;
+    float rest_density = 1.f, gas_constant = 1.f, gamma = 1.f, mass = 1.f, particle_size = 1.f;
+    float xsph = 0.5f, surface_tension = 1.f, viscosity = 0.1f, adhesion = 1.f, vdamp = 1.f;
+    float vel_limit = 5.f, acc_limit = 150.f, dt = 0.01f;
+    float gravity[3] = {0.f, -9.8f, 0.f};
+};
+
+// Derive the device parameter block (FluidParams::setRes and setters,
+// fluidparams.cu:51-213).  Returns false for an unusable domain.
+bool derive_params(const SceneConfig& c, DevParams& out, std::string* err);
+
+struct Scene {
+    int id = -1;
+    uint32_t part_base = 0, n = 0;
+    SceneConfig cfg;
+    DevParams dp{};
+};
+
+enum { ENG_OK = 0, ENG_EINVAL = 1, ENG_ENOMEM = 2, ENG_ECUDA = 3, ENG_ENAN = 4, ENG_ECELL = 7 };
+
+class Engine {
+public:
+    explicit Engine(int device = -1);
+    ~Engine();
+    Engine(const Engine&) = delete;
+    Engine& operator=(const Engine&) = delete;
+
+    // Scene management (only between steps).
+    int add_scene(const SceneConfig& cfg, uint32_t n, int* id_out);
+    int remove_scene(int id);
+    int set_config(int id, const SceneConfig& cfg);
+    const Scene* scene(int id) const;
+    size_t num_scenes() const { return scenes_.size(); }
+    uint64_t total_particles() const;
+
+    // State transfer (host packed xyz float32; device pointers allowed).
+    int set_state(int id, const float* pos, const float* vel, uint32_t n, bool from_device = false);
+    int set_positions(int id, uint32_t first, const float* pos, uint32_t count);
+    int generate_lattice(int id, const LatticeSpec& spec, uint32_t first);
+    int get_state(int id, float* pos, float* colour, float* vel, uint32_t n, bool to_device = false);
+
+    // Advance every live scene by `substeps` substeps (all with their own dt).
+    int step(uint32_t substeps, bool sync = true);
+    int sync();
+
+    // Debug taps (copy to host).  Valid after at least one substep.
+    int debug_enable(bool on);
+    enum Field { F_HASH = 0, F_PERM, F_CELLSTART, F_CELLOCC, F_NBRCOUNT, F_DENSITY, F_PRESSURE, F_SOUNDSPEED,
+                 F_FPRESSURE, F_FTENSION, F_FADHESION, F_FVISCOSITY, F_NORMAL, F_POS_SORTED, F_ACC };
+    int debug_get(int id, int field, void* host, uint64_t count);
+
+    // Options.
+    void set_use_graph(bool on) { use_graph_ = on; graph_dirty_ = true; }
+    cudaStream_t stream() const { return stream_; }
+    const std::string& last_error() const { return err_; }
+    int device() const { return device_; }
+
+    // Per-pass timing with CUDA events (profiling runs; disables the graph).
+    int set_profiling(bool on);
+    int get_pass_times(double* ms_out, int cap, uint64_t* launches);
+    static const char* pass_name(int i);
+    static constexpr int kPasses = 8;
+
+    // Device timers on the engine's stream.
+    int timer_mark(int slot);
+    int timer_elapsed(int a, int b, float* ms);
+
+    // Byte footprint of the arenas (for admission control).
+    static uint64_t bytes_per_particle();
+    static uint64_t bytes_per_cell();
+    uint64_t device_bytes() const { return dev_bytes_; }
+
+private:
+    int fail(int code, const std::string& msg);
+    int cuda_fail(cudaError_t e, const char* what);
+    int ensure_capacity(uint64_t parts, uint64_t cells);
+    int rebuild_layout();
+    int upload_params();
+    int launch_substep(bool profile);
+    int read_status();
+    void free_all();
+    uint32_t alloc_slots(uint32_t n);
+    void free_slots(uint32_t base, uint32_t n);
+    int staging(size_t bytes, float** out);
+    StepArgs args() const;
+
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    std::string err_;
+    std::vector<Scene> scenes_;
+    int next_id_ = 1;
+    // free slot ranges: base -> length
+    std::map<uint32_t, uint32_t> free_;
+    uint64_t pcap_ = 0, ccap_ = 0, slots_end_ = 0;
+    // device arenas
+    float4 *P0_ = nullptr, *P1_ = nullptr, *V0_ = nullptr, *V1_ = nullptr, *V2_ = nullptr, *A0_ = nullptr,
+           *A1_ = nullptr, *S_ = nullptr, *N_ = nullptr;
+    uint32_t *key_ = nullptr, *slot_ = nullptr, *tmp_ = nullptr, *perm_ = nullptr;
+    uint32_t *count_ = nullptr, *start_ = nullptr, *scan_sums_ = nullptr, *status_ = nullptr;
+    uint32_t* dbg_nbr_ = nullptr;
+    float* stage_ = nullptr;           // device staging for packed xyz transfers
+    size_t stage_bytes_ = 0;
+    float4* dbg_forces_ = nullptr;
+    DevParams* d_params_ = nullptr;
+    DevScene* d_scenes_ = nullptr;
+    uint4* d_tiles_ = nullptr;
+    uint64_t scene_cap_ = 0, tile_cap_ = 0;
+    uint64_t dev_bytes_ = 0;
+    // host mirrors
+    DevParams* h_params_ = nullptr;    // pinned
+    uint32_t* h_status_ = nullptr;     // pinned
+    std::vector<DevScene> h_scenes_;
+    std::vector<uint4> h_tiles_;
+    std::vector<uint32_t> cell_base_;
+    uint32_t total_cells_ = 0;
+    bool any_tension_ = false;
+    bool layout_dirty_ = true, params_dirty_ = true, graph_dirty_ = true;
+    bool debug_ = false, use_graph_ = true, profiling_ = false;
+    bool stepped_ = false;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    cudaEvent_t ev_[kPasses + 1] = {};
+    cudaEvent_t timers_[64] = {};
+    double pass_ms_[kPasses] = {};
+    uint64_t prof_substeps_ = 0;
+};
+
+}  // namespace sph

@@ -1,0 +1,127 @@
+// Device-side building blocks of the WCSPH step: box SDF, smoothing kernels,
+// spatial hash.  The library is compiled with -fmad=false: every fused
+// multiply-add below is written out with fmaf() so that the arithmetic is
+// fixed and identical to the CPU oracle's.  The fused points are:
+//   dot(a,b)        = fma(a.z,b.z, fma(a.y,b.y, a.x*b.x))
+//   h2 - r*r        = fma(-r, r, h2)
+//   running sums    = fma(a, b, s)
+// The reference build lets nvcc choose (it contracts by default); results
+// differ from it by a few ulp, within the tolerances of the parity tests.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "sph_types.h"
+
+namespace sph {
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return fmaf(az, bz, fmaf(ay, by, ax * bx));
+}
+
+// Box signed distance, negative inside (boundarySDF, fluidutil.cu:85-102).
+__device__ __forceinline__ float sdf_box(const DevParams& P, float x, float y, float z) {
+    const float qx = fabsf(x - P.box_cx) - P.box_bx;
+    const float qy = fabsf(y - P.box_cy) - P.box_by;
+    const float qz = fabsf(z - P.box_cz) - P.box_bz;
+    const float inner = fminf(fmaxf(qx, fmaxf(qy, qz)), 0.0f);
+    const float px = fmaxf(qx, 0.0f), py = fmaxf(qy, 0.0f), pz = fmaxf(qz, 0.0f);
+    return inner + sqrtf(dot3(px, py, pz, px, py, pz));
+}
+
+// Central-difference SDF normal (boundaryNormalSDF, fluidutil.cu:104-112),
+// normalised as v * (1/sqrt(v.v)).
+__device__ __forceinline__ float3 sdf_normal(const DevParams& P, float x, float y, float z) {
+    const float e = 0.0001f;
+    const float nx = sdf_box(P, x + e, y, z) - sdf_box(P, x - e, y, z);
+    const float ny = sdf_box(P, x, y + e, z) - sdf_box(P, x, y - e, z);
+    const float nz = sdf_box(P, x, y, z + e) - sdf_box(P, x, y, z - e);
+    const float inv = 1.0f / sqrtf(dot3(nx, ny, nz, nx, ny, nz));
+    return make_float3(nx * inv, ny * inv, nz * inv);
+}
+
+// poly6 (fluidkernel.cu:5-8); the cube is formed by multiplication.
+__device__ __forceinline__ float poly6(const DevParams& P, float r) {
+    const float x = fmaf(-r, r, P.h2);
+    return (r >= P.h) ? 0.0f : P.poly6 * (x * x * x);
+}
+// grad poly6 (fluidkernel.cu:10-13)
+__device__ __forceinline__ float grad_poly6(const DevParams& P, float r) {
+    const float x = fmaf(-r, r, P.h2);
+    return (r >= P.h) ? 0.0f : P.grad_poly6 * r * (x * x);
+}
+// grad spiky (fluidkernel.cu:25-28)
+__device__ __forceinline__ float grad_spiky(const DevParams& P, float r) {
+    return (r >= P.h) ? 0.0f : P.grad_spiky * (P.h - r) * (P.h - r);
+}
+// cohesion (fluidkernel.cu:35-38) with the reference's operator precedence:
+// the coefficient times (r > h/2) only selects the branch.
+__device__ __forceinline__ float cohesion_k(const DevParams& P, float r) {
+    if (r >= P.h) return 0.0f;
+    const float sel = P.cohesion * (r > P.halfh ? 1.0f : 0.0f);
+    const float hr = P.h - r;
+    const float hr3 = hr * hr * hr;
+    if (sel != 0.0f) return hr3 * r * r * r;
+    return 2.0f * hr3 * r * r * r - P.h6 * 0.0156f;
+}
+// boundaryDensity (fluidkernel.cu:45-67)
+__device__ __forceinline__ float boundary_density(const DevParams& P, float d) {
+    if ((d > P.h) || (d < 0.0f)) return 0.0f;
+    const float c = -d, c2 = c * c, c3 = c2 * c, c4 = c3 * c, c6 = c3 * c3;
+    const float poly = c3 * (35.0f * c6 - 180.0f * c4 * P.h2 + 378.0f * c2 * P.h4 - 420.0f * P.h6)
+                     + 315.0f * c * P.h8 + 128.0f * P.h9;
+    return 1.0f - 0.0039062f * P.invh9 * poly;
+}
+
+// Grid coordinates of a position: floor(p * inv_cell) converted with
+// round-toward-zero saturation (grid_from_point, fluidutil.cu:15-18).
+__device__ __forceinline__ int3 grid_of(const DevParams& P, float x, float y, float z) {
+    return make_int3(__float2int_rz(floorf(x * P.inv_cell)), __float2int_rz(floorf(y * P.inv_cell)),
+                     __float2int_rz(floorf(z * P.inv_cell)));
+}
+__device__ __forceinline__ bool grid_inside(const DevParams& P, int3 g) {
+    return g.x >= 0 && g.x < (int)P.gx && g.y >= 0 && g.y < (int)P.gy && g.z >= 0 && g.z < (int)P.gz;
+}
+// Scene-local cell index, or P.ncells (the scene's NULL bucket) outside the
+// grid (cell_from_grid, fluidutil.cu:29-39, NULL_HASH -> bucket ncells).
+__device__ __forceinline__ uint32_t cell_of(const DevParams& P, float x, float y, float z) {
+    const int3 g = grid_of(P, x, y, z);
+    return grid_inside(P, g) ? (uint32_t)g.x + (uint32_t)g.y * P.gx + (uint32_t)g.z * P.gxy : P.ncells;
+}
+
+// Visit the candidate neighbours of a particle in grid cell g: the 27 cells
+// around it, clipped at the grid edge (fluidphysics.cu:30-34).  Cells
+// (x-1..x+1, y, z) are consecutive in the x-fastest order and particles are
+// sorted by cell, so each (y,z) row is one contiguous slot range.
+// start[] is the exclusive scan of cell counts over the packed cell arena;
+// delta maps it to particle slots.
+template <class F>
+__device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_t* __restrict__ start,
+                                               uint32_t cell_base, uint32_t delta, int3 g, F&& f) {
+    const int x0 = max(g.x - 1, 0), x1 = min(g.x + 1, (int)P.gx - 1);
+    const int z0 = max(g.z - 1, 0), z1 = min(g.z + 1, (int)P.gz - 1);
+    const int y0 = max(g.y - 1, 0), y1 = min(g.y + 1, (int)P.gy - 1);
+    for (int z = z0; z <= z1; ++z) {
+        for (int y = y0; y <= y1; ++y) {
+            const uint32_t row = cell_base + (uint32_t)y * P.gx + (uint32_t)z * P.gxy;
+            const uint32_t jb = __ldg(start + row + x0) + delta;
+            const uint32_t je = __ldg(start + row + x1 + 1) + delta;
+            for (uint32_t j = jb; j < je; ++j) f(j);
+        }
+    }
+}
+
+// Counter-based generator for lattice jitter: splitmix64 (Steele, Lea and
+// Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014).
+__host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    uint64_t z = x + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+// Uniform float in [0,1) from the top 24 bits of draw `ctr` of stream `seed`.
+__host__ __device__ __forceinline__ float uniform01(uint64_t seed, uint64_t ctr) {
+    const uint64_t z = splitmix64(seed ^ (ctr * 0xD1B54A32D192ED03ull));
+    return (float)(uint32_t)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+}  // namespace sph

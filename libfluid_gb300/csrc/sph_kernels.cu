@@ -1,0 +1,633 @@
+// sm_103a kernels of the WCSPH substep.
+//
+// One substep (the body of FluidSystem::advance, fluidsystem.cu:301-398) is:
+//   memset counts -> k_hash -> scan (3 kernels) -> k_scatter -> k_rank_gather
+//   -> k_density -> [k_normals] -> k_force_integrate -> k_xsph
+// Every kernel is scene-aware: a launch covers the tiles of all live scenes,
+// so the plain step is the batched step with one scene.
+//
+// State buffers (float4 per particle, slots indexed by the arena):
+//   P0,V0,A0  state between substeps (P0.w = density of the last substep)
+//   P1,V1,A1  state gathered into cell order
+//   S         (rho, p, c^2, 0) per sorted slot
+//   N         surface normals (only when a scene has surface tension)
+//   V2        post-integration velocity (read by XSPH, which writes V0)
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "sph_types.h"
+#include "sph_device.cuh"
+#include "sph_kernels.h"
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// Spatial hash + cell counts (hash.cu:10-27 and the fill at
+// fluidsystem.cu:304-306).  Equal keys inside a warp are combined with
+// __match_any_sync so one atomic serves each group; the slot a particle gets
+// inside its cell is provisional (atomic order) and is made stable by
+// k_rank_gather.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_hash(const DevParams* __restrict__ params,
+                                                   const DevScene* __restrict__ scenes,
+                                                   const uint4* __restrict__ tiles,
+                                                   const float4* __restrict__ P, uint32_t* __restrict__ count,
+                                                   uint32_t* __restrict__ key, uint32_t* __restrict__ slot,
+                                                   uint32_t* __restrict__ status) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t i = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const DevParams& pp = params[t.x];
+    const float4 p = P[i];
+    const uint32_t local = cell_of(pp, p.x, p.y, p.z);
+    if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(status, SPH_STATUS_NONFINITE);
+    const uint32_t gkey = sc.cell_base + local;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned active = __activemask();
+    const unsigned peers = __match_any_sync(active, gkey);
+    const int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&count[gkey], (uint32_t)__popc(peers));
+    base = __shfl_sync(active, base, leader);
+    key[i] = local;
+    slot[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of cell counts -> cell starts (fluidsystem.cu:316).
+// Reduce-then-scan: 4096 counts per tile.
+// ---------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    const unsigned lane = threadIdx.x & 31u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (unsigned)o) v += u;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __restrict__ in, uint32_t n,
+                                                              uint32_t* __restrict__ sums) {
+    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const uint32_t idx = base + k;
+        if (idx < n) s += in[idx];
+    }
+    __shared__ uint32_t red[SCAN_THREADS / 32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31u) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t w = (threadIdx.x < SCAN_THREADS / 32) ? red[threadIdx.x] : 0u;
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (threadIdx.x == 0) sums[blockIdx.x] = w;
+    }
+}
+
+// Single block: exclusive scan of up to 1024*32 tile sums, in place.
+__global__ void __launch_bounds__(1024) k_scan_top(uint32_t* __restrict__ sums, uint32_t nt) {
+    constexpr int ITEMS = 32;
+    uint32_t v[ITEMS];
+    const uint32_t base = threadIdx.x * ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        v[k] = (base + k < nt) ? sums[base + k] : 0u;
+        s += v[k];
+    }
+    __shared__ uint32_t warp_tot[32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_incl_scan(s);
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = warp_tot[lane];
+        const uint32_t wi = warp_incl_scan(w);
+        warp_tot[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = warp_tot[warp] + inc - s;
+#pragma unroll
+    for (int k = 0; k < ITEMS; ++k) {
+        if (base + k < nt) sums[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __restrict__ in, uint32_t n,
+                                                            const uint32_t* __restrict__ sums,
+                                                            uint32_t* __restrict__ out) {
+    const uint32_t base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const uint32_t idx = base + k;
+        v[k] = (idx < n) ? in[idx] : 0u;
+        s += v[k];
+    }
+    __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_incl_scan(s);
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = (lane < SCAN_THREADS / 32) ? warp_tot[lane] : 0u;
+        const uint32_t wi = warp_incl_scan(w);
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = wi - w;
+    }
+    __syncthreads();
+    uint32_t run = sums[blockIdx.x] + warp_tot[warp] + inc - s;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const uint32_t idx = base + k;
+        if (idx < n) out[idx] = run;
+        run += v[k];
+        if (idx + 1 == n) out[n] = run;   // total after the last cell
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scatter: provisional slot of each particle in cell order.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_scatter(const DevScene* __restrict__ scenes,
+                                                      const uint4* __restrict__ tiles,
+                                                      const uint32_t* __restrict__ start,
+                                                      const uint32_t* __restrict__ key,
+                                                      const uint32_t* __restrict__ slot,
+                                                      uint32_t* __restrict__ tmp) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t i = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const uint32_t s0 = __ldg(start + sc.cell_base);
+    const uint32_t c = sc.cell_base + key[i];
+    tmp[sc.part_base + (__ldg(start + c) - s0) + slot[i]] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Stable rank inside the cell + gather into cell order.  thrust::sort_by_key
+// over u32 keys (fluidsystem.cu:309-313) is a stable radix sort: within a cell
+// particles keep their current order.  Each sorted slot's final position is
+// the cell start plus the number of cell members with a smaller current
+// index, which reproduces that permutation exactly.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __restrict__ scenes,
+                                                          const uint4* __restrict__ tiles,
+                                                          const uint32_t* __restrict__ start,
+                                                          const uint32_t* __restrict__ key,
+                                                          const uint32_t* __restrict__ tmp,
+                                                          const float4* __restrict__ P0,
+                                                          const float4* __restrict__ V0,
+                                                          const float4* __restrict__ A0,
+                                                          float4* __restrict__ P1, float4* __restrict__ V1,
+                                                          float4* __restrict__ A1, uint32_t* __restrict__ perm,
+                                                          uint32_t* __restrict__ status) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t g = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const uint32_t i = tmp[g];
+    const uint32_t s0 = __ldg(start + sc.cell_base);
+    const uint32_t c = sc.cell_base + __ldg(key + i);
+    const uint32_t b = sc.part_base + (__ldg(start + c) - s0);
+    const uint32_t e = sc.part_base + (__ldg(start + c + 1) - s0);
+    if (e - b > SPH_MAX_CELL_OCC) {
+        atomicOr(status, SPH_STATUS_CELL_OVERFLOW);
+        return;
+    }
+    uint32_t rank = 0;
+    for (uint32_t m = b; m < e; ++m) rank += (__ldg(tmp + m) < i) ? 1u : 0u;
+    const uint32_t f = b + rank;
+    perm[f] = i;
+    P1[f] = P0[i];
+    V1[f] = V0[i];
+    A1[f] = A0[i];
+}
+
+// ---------------------------------------------------------------------------
+// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restrict__ params,
+                                                      const DevScene* __restrict__ scenes,
+                                                      const uint4* __restrict__ tiles,
+                                                      const uint32_t* __restrict__ start,
+                                                      const float4* __restrict__ P1, float4* __restrict__ S,
+                                                      uint32_t* __restrict__ nbr_out) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t k = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const DevParams& pp = params[t.x];
+    const float4 p = P1[k];
+    const int3 g = grid_of(pp, p.x, p.y, p.z);
+    if (!grid_inside(pp, g)) {
+        S[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (nbr_out) nbr_out[k] = 0;
+        return;
+    }
+    const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
+    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6;
+    float sum = 0.0f;
+    uint32_t cnt = 0;
+    for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+        const float4 q = __ldg(P1 + j);
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        const float rr = dot3(dx, dy, dz, dx, dy, dz);
+        if (rr <= h2 && j != k) {
+            const float r = sqrtf(rr);
+            const float x = fmaf(-r, r, h2);
+            const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
+            sum = fmaf(mass, w, sum);
+            cnt++;
+        }
+    });
+    const float d = fabsf(sdf_box(pp, p.x, p.y, p.z));
+    float corr = sum;
+    if (d < pp.h) corr = fmaf(pp.rest_density, 1.0f - boundary_density(pp, d), corr);
+    const float rho = (sum == 0.0f) ? pp.rest_density : corr;
+    const float ratio = corr * pp.inv_rest_density;
+    const float prs = (corr == 0.0f) ? 0.0f : pp.eos_k * (powf(ratio, pp.gamma) - 1.0f);
+    const float cs = pp.gas_constant * powf(ratio, pp.gamma - 1.0f);
+    S[k] = make_float4(rho, prs, cs, 0.0f);
+    if (nbr_out) nbr_out[k] = cnt;
+}
+
+// ---------------------------------------------------------------------------
+// Surface normals (computeNormals, fluidphysics.cu:154-210).  Only launched
+// for scenes with surface tension: with sigma == 0 the normals enter the
+// force only through sigma * (...), which is exactly zero.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restrict__ params,
+                                                      const DevScene* __restrict__ scenes,
+                                                      const uint4* __restrict__ tiles,
+                                                      const uint32_t* __restrict__ start,
+                                                      const float4* __restrict__ P1,
+                                                      const float4* __restrict__ S, float4* __restrict__ N) {
+    const uint4 t = tiles[blockIdx.x];
+    const DevParams& pp = params[t.x];
+    if (!(pp.flags & 1u)) return;
+    if (threadIdx.x >= t.z) return;
+    const uint32_t k = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const float4 p = P1[k];
+    const int3 g = grid_of(pp, p.x, p.y, p.z);
+    if (!grid_inside(pp, g)) {
+        N[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+        const float4 q = __ldg(P1 + j);
+        const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
+        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (r2 <= pp.h2 && r2 > pp.eps && j != k) {
+            const float rhoj = __ldg(&S[j].x);
+            if (rhoj > pp.eps) {
+                const float r = sqrtf(r2);
+                const float s = pp.mass * grad_poly6(pp, r);
+                const float den = rhoj * r;
+                sx = sx + (s * rx) / den;
+                sy = sy + (s * ry) / den;
+                sz = sz + (s * rz) / den;
+            }
+        }
+    });
+    N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Forces (computeAllForces, fluidphysics.cu:215-352) fused with the leapfrog
+// integrator and box boundary (LeapfrogIntegratorOperator,
+// fluidintegrator.cu:11-70).  Reads cell-order state (P1,V1,A1,S,N), writes
+// the integrated state to P0 (w = density), V2, A0.  The integrator sums the
+// force buffers in the reference's order, which after the swapped arguments
+// at fluidsystem.cu:352-364 is ((pressure + tension) + viscosity) + adhesion.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_force_integrate(const DevParams* __restrict__ params,
+                                                              const DevScene* __restrict__ scenes,
+                                                              const uint4* __restrict__ tiles,
+                                                              const uint32_t* __restrict__ start,
+                                                              const float4* __restrict__ P1,
+                                                              const float4* __restrict__ V1,
+                                                              const float4* __restrict__ A1,
+                                                              const float4* __restrict__ S,
+                                                              const float4* __restrict__ N,
+                                                              float4* __restrict__ P0, float4* __restrict__ V2,
+                                                              float4* __restrict__ A0,
+                                                              float4* __restrict__ dbg_forces) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t k = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const DevParams& pp = params[t.x];
+    const float4 pi = P1[k];
+    const float4 vi = V1[k];
+    const float4 si = S[k];
+    const int3 g = grid_of(pp, pi.x, pi.y, pi.z);
+    const bool tension = (pp.flags & 1u) != 0u;
+    float fpx = 0.f, fpy = 0.f, fpz = 0.f;   // pressure
+    float fvx = 0.f, fvy = 0.f, fvz = 0.f;   // "viscosity" (pressure re-added)
+    float ftx = 0.f, fty = 0.f, ftz = 0.f;   // tension
+    float fax = 0.f, fay = 0.f, faz = 0.f;   // adhesion
+    if (grid_inside(pp, g)) {
+        const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
+        const float ri = si.x, pri = si.y, csi = si.z;
+        float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (tension) ni = N[k];
+        const float h2 = pp.h2, eps = pp.eps;
+        for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+            const float4 pj = __ldg(P1 + j);
+            const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
+            const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+            if (r2 <= h2 && r2 > eps && j != k) {
+                const float4 sj = __ldg(S + j);
+                if (sj.x > eps) {
+                    const float4 vj = __ldg(V1 + j);
+                    const float r = sqrtf(r2);
+                    const float inv_r = 1.0f / r;
+                    const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
+                    float Pi = 0.0f;
+                    if (ux < 0.0f) {
+                        const float mu = (pp.h * ux) / (r2 + pp.visc_eps);
+                        Pi = (-pp.viscosity * (csi + sj.z) * mu) / (ri + sj.x);
+                    }
+                    const float mid = sj.y / (ri * ri) + pri / (sj.x * sj.x);
+                    const float s = pp.mass * grad_spiky(pp, r);
+                    const float cx = (s * rx) * inv_r, cy = (s * ry) * inv_r, cz = (s * rz) * inv_r;
+                    fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
+                    const float mp = mid + Pi;
+                    fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
+                    if (tension) {
+                        // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
+                        // sigma == 0 the tension force is sigma * (finite sum) = 0, so
+                        // the term is skipped.
+                        const float sc2 = -pp.mass * pp.mass * cohesion_k(pp, r);
+                        const float hx = (sc2 * rx) * inv_r, hy = (sc2 * ry) * inv_r, hz = (sc2 * rz) * inv_r;
+                        const float4 nj = __ldg(N + j);
+                        const float sm = -pp.surface_tension * pp.mass;
+                        const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
+                        const float tr = 2.0f * pp.rest_density;
+                        const float den = ri + ri;
+                        ftx = ftx + (tr * (hx + kx)) / den;
+                        fty = fty + (tr * (hy + ky)) / den;
+                        ftz = ftz + (tr * (hz + kz)) / den;
+                    }
+                }
+            }
+        });
+        fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
+        ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
+        const float z = -fminf(sdf_box(pp, pi.x, pi.y, pi.z), 0.0f) * 0.25f * pp.inv_particle_size;
+        if (z < 1.0f) {
+            const float3 nb = sdf_normal(pp, pi.x, pi.y, pi.z);
+            const float denom = 1.0f / powf(1.0f - z, 3.0f);
+            const float a = pp.adhesion * ri * pp.inv_rest_density * denom;
+            fax = a * nb.x; fay = a * nb.y; faz = a * nb.z;
+        }
+    }
+    if (dbg_forces) {
+        dbg_forces[4 * (size_t)k + 0] = make_float4(fpx, fpy, fpz, 0.f);
+        dbg_forces[4 * (size_t)k + 1] = make_float4(ftx, fty, ftz, 0.f);
+        dbg_forces[4 * (size_t)k + 2] = make_float4(fax, fay, faz, 0.f);
+        dbg_forces[4 * (size_t)k + 3] = make_float4(fvx, fvy, fvz, 0.f);
+    }
+    // ---- leapfrog integrator + boundary ----
+    const float4 ai = A1[k];
+    const float Fx = ((fpx + ftx) + fvx) + fax;
+    const float Fy = ((fpy + fty) + fvy) + fay;
+    const float Fz = ((fpz + ftz) + fvz) + faz;
+    float anx = fmaf(Fx, pp.mass, pp.grav_x), any = fmaf(Fy, pp.mass, pp.grav_y), anz = fmaf(Fz, pp.mass, pp.grav_z);
+    float sq = dot3(anx, any, anz, anx, any, anz);
+    if (sq > pp.acc_limit2) {
+        const float s = pp.acc_limit / sqrtf(sq);
+        anx = anx * s; any = any * s; anz = anz * s;
+    }
+    float px = pi.x + fmaf(vi.x, pp.dt, (0.5f * ai.x) * pp.dtdt);
+    float py = pi.y + fmaf(vi.y, pp.dt, (0.5f * ai.y) * pp.dtdt);
+    float pz = pi.z + fmaf(vi.z, pp.dt, (0.5f * ai.z) * pp.dtdt);
+    float vx = fmaf(0.5f * (ai.x + anx), pp.dt, vi.x);
+    float vy = fmaf(0.5f * (ai.y + any), pp.dt, vi.y);
+    float vz = fmaf(0.5f * (ai.z + anz), pp.dt, vi.z);
+    sq = dot3(vx, vy, vz, vx, vy, vz);
+    if (sq > pp.vel_limit2) {
+        const float s = pp.vel_limit / sqrtf(sq);
+        vx = vx * s; vy = vy * s; vz = vz * s;
+    }
+    const float d = sdf_box(pp, px, py, pz);
+    if (d > -pp.particle_size) {
+        const float3 nb = sdf_normal(pp, px, py, pz);
+        const float s = -(d + pp.particle_size);
+        px = fmaf(s, nb.x, px); py = fmaf(s, nb.y, py); pz = fmaf(s, nb.z, pz);
+        const float kk = (1.0f + pp.vdamp) * dot3(nb.x, nb.y, nb.z, vx, vy, vz);
+        vx = fmaf(-kk, nb.x, vx); vy = fmaf(-kk, nb.y, vy); vz = fmaf(-kk, nb.z, vz);
+    }
+    P0[k] = make_float4(px, py, pz, si.x);
+    V2[k] = make_float4(vx, vy, vz, 0.f);
+    A0[k] = make_float4(anx, any, anz, 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// XSPH velocity smoothing (correctVelocityXSPH, fluidphysics.cu:355-409):
+// post-integration positions, this substep's cell lists and densities.  The
+// reference updates velocities in place while neighbours read them (a race);
+// here reads see V2 and the result goes to V0 (Jacobi).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_xsph(const DevParams* __restrict__ params,
+                                                   const DevScene* __restrict__ scenes,
+                                                   const uint4* __restrict__ tiles,
+                                                   const uint32_t* __restrict__ start,
+                                                   const float4* __restrict__ P1,
+                                                   const float4* __restrict__ P0,
+                                                   const float4* __restrict__ V2, float4* __restrict__ V0) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t k = t.y + threadIdx.x;
+    const DevScene sc = scenes[t.x];
+    const DevParams& pp = params[t.x];
+    const float4 vi = V2[k];
+    const float4 old = P1[k];   // the cell this particle was sorted into
+    const int3 g = grid_of(pp, old.x, old.y, old.z);
+    if (!grid_inside(pp, g)) {
+        V0[k] = vi;
+        return;
+    }
+    const float4 pi = P0[k];    // post-integration position, w = density
+    const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
+    const float h2 = pp.h2, h = pp.h, c6 = pp.poly6, two_m = pp.two_mass, eps = pp.eps;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+        const float4 q = __ldg(P0 + j);
+        const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+        const float rr = dot3(dx, dy, dz, dx, dy, dz);
+        const float rs = pi.w + q.w;
+        if (rr <= h2 && rs > eps && j != k) {
+            const float r = sqrtf(rr);
+            const float x = fmaf(-r, r, h2);
+            const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
+            const float coeff = w * (two_m / rs);
+            const float4 vj = __ldg(V2 + j);
+            sx = fmaf(coeff, vj.x - vi.x, sx);
+            sy = fmaf(coeff, vj.y - vi.y, sy);
+            sz = fmaf(coeff, vj.z - vi.z, sz);
+        }
+    });
+    V0[k] = make_float4(fmaf(pp.xsph, sx, vi.x), fmaf(pp.xsph, sy, vi.y), fmaf(pp.xsph, sz, vi.z), 0.f);
+}
+
+// ---------------------------------------------------------------------------
+// Host<->device layout helpers and the lattice generator.
+// ---------------------------------------------------------------------------
+__global__ void k_unpack_state(const float* __restrict__ pos, const float* __restrict__ vel, uint32_t n,
+                               uint32_t base, float4* __restrict__ P0, float4* __restrict__ V0,
+                               float4* __restrict__ A0, float4* __restrict__ S) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t s = base + i;
+    P0[s] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.f);
+    V0[s] = vel ? make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    A0[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    S[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Overwrite positions of slots [base, base+n) keeping the rest of the state
+// (createFluidBlock writes m_Points element by element, fluidsystem.cu:119-123).
+__global__ void k_set_positions(const float* __restrict__ pos, uint32_t n, uint32_t base, float4* __restrict__ P0) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 old = P0[base + i];
+    P0[base + i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], old.w);
+}
+
+// Export: positions, density colour (DensityColourOperator, fluidutil.cu:67-80)
+// and velocities, packed xyz.
+__global__ void k_pack_state(const float4* __restrict__ P0, const float4* __restrict__ V0, uint32_t n,
+                             uint32_t base, float inv_rest_density, float* __restrict__ pos,
+                             float* __restrict__ colour, float* __restrict__ vel) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = P0[base + i];
+    const float4 v = V0[base + i];
+    if (pos) { pos[3 * i] = p.x; pos[3 * i + 1] = p.y; pos[3 * i + 2] = p.z; }
+    if (vel) { vel[3 * i] = v.x; vel[3 * i + 1] = v.y; vel[3 * i + 2] = v.z; }
+    if (colour) {
+        const float ratio = p.w * inv_rest_density;
+        float r = 1.0f, gg = 0.0f, b = 0.0f;
+        if (ratio < 1.0f) { r = 0.0f; gg = ratio; b = 1.0f - ratio; }
+        else if (ratio < 2.0f) { r = ratio - 1.0f; gg = 2.0f - ratio; b = 0.0f; }
+        colour[3 * i] = r; colour[3 * i + 1] = gg; colour[3 * i + 2] = b;
+    }
+}
+
+// Lattice block with seeded jitter; site (ix,iy,iz) -> particle
+// (ix*ny + iy)*nz + iz.  Coordinate: lo + (i + 0.5)*spacing + (2u-1)*jitter.
+__global__ void k_lattice(LatticeSpec spec, uint32_t base, float4* __restrict__ P0, float4* __restrict__ V0,
+                          float4* __restrict__ A0, float4* __restrict__ S) {
+    const uint32_t n = spec.nx * spec.ny * spec.nz;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t iz = i % spec.nz, iy = (i / spec.nz) % spec.ny, ix = i / (spec.nz * spec.ny);
+    const uint32_t idx[3] = {ix, iy, iz};
+    float c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float u = uniform01(spec.seed, 3ull * i + a);
+        const float j = (2.0f * u - 1.0f) * spec.jitter;
+        c[a] = (spec.lo[a] + ((float)idx[a] + 0.5f) * spec.spacing) + j;
+    }
+    const uint32_t s = base + i;
+    P0[s] = make_float4(c[0], c[1], c[2], 0.f);
+    V0[s] = make_float4(spec.vel[0], spec.vel[1], spec.vel[2], 0.f);
+    A0[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    S[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Sorted hash for the debug tap: key of the particle now at each slot, with
+// the NULL bucket reported as NULL_HASH (m_Hash after the sort).
+__global__ void k_sorted_keys(const uint32_t* __restrict__ key, const uint32_t* __restrict__ perm, uint32_t n,
+                              uint32_t base, uint32_t ncells, uint32_t* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = key[perm[base + i]];
+    out[i] = (k == ncells) ? SPH_NULL_HASH : k;
+}
+
+// ---------------------------------------------------------------------------
+// Launch wrappers.
+// ---------------------------------------------------------------------------
+cudaError_t launch_hash(const StepArgs& a, cudaStream_t st) {
+    k_hash<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.P0, a.count, a.key, a.slot, a.status);
+    return cudaGetLastError();
+}
+cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
+    const uint32_t n = a.total_cells;
+    const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nt > 1024u * 32u) return cudaErrorInvalidValue;
+    k_scan_reduce<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, a.scan_sums);
+    k_scan_top<<<1, 1024, 0, st>>>(a.scan_sums, nt);
+    k_scan_down<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, a.scan_sums, a.start);
+    return cudaGetLastError();
+}
+cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
+    k_scatter<<<a.ntiles, SPH_TILE, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
+    k_rank_gather<<<a.ntiles, SPH_TILE, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.P1,
+                                                 a.V1, a.A1, a.perm, a.status);
+    return cudaGetLastError();
+}
+cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
+    k_density<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.dbg_nbr);
+    return cudaGetLastError();
+}
+cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
+    k_normals<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.N);
+    return cudaGetLastError();
+}
+cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
+    k_force_integrate<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S,
+                                                     a.N, a.P0, a.V2, a.A0, a.dbg_forces);
+    return cudaGetLastError();
+}
+cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st) {
+    k_xsph<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.V0);
+    return cudaGetLastError();
+}
+cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,
+                          float4* A0, float4* S, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_unpack_state<<<(n + 255) / 256, 256, 0, st>>>(pos, vel, n, base, P0, V0, A0, S);
+    return cudaGetLastError();
+}
+cudaError_t launch_set_positions(const float* pos, uint32_t n, uint32_t base, float4* P0, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_set_positions<<<(n + 255) / 256, 256, 0, st>>>(pos, n, base, P0);
+    return cudaGetLastError();
+}
+cudaError_t launch_pack(const float4* P0, const float4* V0, uint32_t n, uint32_t base, float inv_rest_density,
+                        float* pos, float* colour, float* vel, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_pack_state<<<(n + 255) / 256, 256, 0, st>>>(P0, V0, n, base, inv_rest_density, pos, colour, vel);
+    return cudaGetLastError();
+}
+cudaError_t launch_lattice(const LatticeSpec& spec, uint32_t base, float4* P0, float4* V0, float4* A0, float4* S,
+                           cudaStream_t st) {
+    const uint32_t n = spec.nx * spec.ny * spec.nz;
+    if (n == 0) return cudaSuccess;
+    k_lattice<<<(n + 255) / 256, 256, 0, st>>>(spec, base, P0, V0, A0, S);
+    return cudaGetLastError();
+}
+cudaError_t launch_sorted_keys(const uint32_t* key, const uint32_t* perm, uint32_t n, uint32_t base,
+                               uint32_t ncells, uint32_t* out, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_sorted_keys<<<(n + 255) / 256, 256, 0, st>>>(key, perm, n, base, ncells, out);
+    return cudaGetLastError();
+}
+
+}  // namespace sph

@@ -1,0 +1,46 @@
+// Launch interface of the substep kernels (sph_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "sph_types.h"
+
+namespace sph {
+
+// Device pointers and sizes for one substep over all live scenes.
+struct StepArgs {
+    const DevParams* params;   // one per scene (indexed by scene table position)
+    const DevScene* scenes;
+    const uint4* tiles;        // (scene, first slot, count, 0)
+    uint32_t ntiles;
+    uint32_t total_cells;      // packed cell arena size including NULL buckets
+    float4 *P0, *V0, *A0;      // state
+    float4 *P1, *V1, *A1;      // cell-ordered state
+    float4 *V2;                // post-integration velocity
+    float4 *S;                 // (rho, p, c^2, 0)
+    float4 *N;                 // normals
+    uint32_t *count, *start, *scan_sums;
+    uint32_t *key, *slot, *tmp, *perm;
+    uint32_t *status;
+    uint32_t *dbg_nbr;         // optional: neighbour counts per sorted slot
+    float4 *dbg_forces;        // optional: 4 force vectors per sorted slot
+};
+
+cudaError_t launch_hash(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_scan(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_sort(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_density(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_normals(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_force(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st);
+
+cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,
+                          float4* A0, float4* S, cudaStream_t st);
+cudaError_t launch_set_positions(const float* pos, uint32_t n, uint32_t base, float4* P0, cudaStream_t st);
+cudaError_t launch_pack(const float4* P0, const float4* V0, uint32_t n, uint32_t base, float inv_rest_density,
+                        float* pos, float* colour, float* vel, cudaStream_t st);
+cudaError_t launch_lattice(const LatticeSpec& spec, uint32_t base, float4* P0, float4* V0, float4* A0, float4* S,
+                           cudaStream_t st);
+cudaError_t launch_sorted_keys(const uint32_t* key, const uint32_t* perm, uint32_t n, uint32_t base,
+                               uint32_t ncells, uint32_t* out, cudaStream_t st);
+
+}  // namespace sph

@@ -1,0 +1,68 @@
+// Plain-old-data types shared by host code and sm_103a kernels.
+//
+// One scene = one independent fluid system (a FluidSystem in the reference,
+// libfluid/include/fluidsystem.h:16-126).  The reference keeps one parameter
+// block per process in __constant__ memory (fluidparams.cu:6); here every
+// scene has its own DevParams in global memory so that many scenes can be
+// advanced by one launch per pass.
+#pragma once
+#include <stdint.h>
+
+#define SPH_NULL_HASH 0xFFFFFFFFu   // fluiddefines.h:12 (UINT_MAX)
+
+// Derived per-scene parameters (the FluidParamData of fluidparams.cuh:16-69,
+// generalised to a rectangular box [0,L]^3 with cell size h).
+struct DevParams {
+    // grid: cell = floor(p * inv_cell) per axis, linearised x fastest
+    uint32_t gx, gy, gz, gxy;     // grid dims and gx*gy
+    uint32_t ncells;              // gx*gy*gz; the scene's NULL bucket is cell ncells
+    float inv_cell;               // float(res) for the unit cube
+    // box signed distance: d = |p - c| - b (fluidutil.cu:85-102)
+    float box_cx, box_cy, box_cz, box_bx, box_by, box_bz;
+    // smoothing length and kernel constants (fluidparams.cu:51-89)
+    float h, halfh, h2, h4, h6, h8, h9, invh9;
+    float poly6, grad_poly6, grad_spiky, cohesion;
+    float visc_eps;               // 0.01*h^2 (fluidphysics.cu:279), rounded to float once
+    // fluid
+    float rest_density, inv_rest_density, gas_constant, gamma, eos_k;  // eos_k = B*rho0/gamma
+    float mass, two_mass, particle_size, inv_particle_size;
+    float dt, dtdt;
+    float xsph, surface_tension, viscosity, adhesion, vdamp;
+    float vel_limit, acc_limit, vel_limit2, acc_limit2;
+    float grav_x, grav_y, grav_z;
+    float eps;                    // FLT_MIN (fluidparams.cu:48)
+    uint32_t flags;               // bit0: surface tension active (normals pass needed)
+    uint32_t pad_[3];
+};
+
+// Scene placement in the engine's arenas.
+struct DevScene {
+    uint32_t part_base;   // first particle slot of the scene
+    uint32_t n;           // particle count
+    uint32_t cell_base;   // first cell of the scene in the packed cell arena
+    uint32_t ncells;      // real cells; the NULL bucket follows at cell_base+ncells
+};
+
+// A tile: up to SPH_TILE consecutive particle slots of one scene.
+// x = scene, y = first slot, z = count, w = 0.
+#define SPH_TILE 256
+
+// Status bits raised by kernels (read back after a step).
+#define SPH_STATUS_CELL_OVERFLOW 0x1u   // a cell held more particles than the rank pass supports
+#define SPH_STATUS_NONFINITE     0x2u   // a non-finite position appeared
+
+// Maximum particles one cell (or a scene's NULL bucket) may hold.  The
+// reference cannot launch more than 1024 threads per cell block
+// (fluidsystem.cu:322); this build supports 8x that.
+#define SPH_MAX_CELL_OCC 8192u
+
+// Lattice block generator (a dam-break fluid block with seeded jitter).
+struct LatticeSpec {
+    float lo[3];          // block corner
+    float spacing;        // lattice spacing
+    uint32_t nx, ny, nz;  // lattice sites per axis (x outermost, z innermost)
+    float jitter;         // uniform jitter amplitude (+/-)
+    float vel[3];         // initial velocity
+    uint32_t pad_;
+    uint64_t seed;
+};
