@@ -169,6 +169,23 @@ int sph_timer_elapsed(sph_system* s, int a, int b, float* ms);
 const char* sph_last_error(const sph_system* s);
 const char* sph_version(void);
 
+/* ---- allocation-free cell-start scan ------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (an application that owns all device memory through its own arena, or a
+ * frame loop where an allocation would stall the device): exclusive scan of
+ * n per-cell particle counts (device u32[n]) into cell starts (device
+ * u32[n+1], starts[n] = total), the step fluidsystem.cu:316 performs, with
+ * its scratch in a fixed 128 KiB array inside the library instead of a
+ * cudaMalloc.  n must be 1..SPH_NOALLOC_MAX_CELLS, else SPH_EINVAL.
+ * Enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) on
+ * the current device; it does not synchronise.  The first call on each
+ * device looks up the scratch address (cudaGetSymbolAddress), so make that
+ * first call before any stream capture.  Every call shares the scratch:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+#define SPH_NOALLOC_MAX_TILES 32768u
+#define SPH_NOALLOC_MAX_CELLS (SPH_NOALLOC_MAX_TILES * 4096u)
+int sph_scan_cells_noalloc(const uint32_t* counts, uint32_t n, uint32_t* starts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

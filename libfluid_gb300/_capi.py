@@ -91,6 +91,7 @@ SIGNATURES = [
     ("sph_timer_elapsed", _I, [_P, _I, _I, _FP]),
     ("sph_last_error", C.c_char_p, [_P]),
     ("sph_version", C.c_char_p, []),
+    ("sph_scan_cells_noalloc", _I, [_P, _U32, _P, _P]),
 ]
 
 

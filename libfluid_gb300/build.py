@@ -45,7 +45,7 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{INCLUDE}", f"-I{CSRC}",
              f"-I{os.path.join(CUDA, 'include')}"]
 
-KERNEL_SOURCES = ["sph_kernels.cu"]
+KERNEL_SOURCES = ["sph_kernels.cu", "sph_noalloc.cu"]
 HOST_SOURCES = ["engine.cpp", "capi.cpp"]
 
 LIB_SPH = os.path.join(PKG, "libsph_gb300.so")

@@ -576,6 +576,15 @@ cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
     k_scan_down<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, a.scan_sums, a.start);
     return cudaGetLastError();
 }
+cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,
+                            cudaStream_t st) {
+    const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (n == 0 || nt > 1024u * 32u) return cudaErrorInvalidValue;
+    k_scan_reduce<<<nt, SCAN_THREADS, 0, st>>>(counts, n, tile_sums);
+    k_scan_top<<<1, 1024, 0, st>>>(tile_sums, nt);
+    k_scan_down<<<nt, SCAN_THREADS, 0, st>>>(counts, n, tile_sums, starts);
+    return cudaGetLastError();
+}
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
     k_scatter<<<a.ntiles, SPH_TILE, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
     k_rank_gather<<<a.ntiles, SPH_TILE, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.P1,

@@ -27,6 +27,10 @@ struct StepArgs {
 
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st);
+// Exclusive scan of counts[0,n) into starts[0,n] with caller-provided tile
+// sums (ceil(n/4096) entries, at most 32768).
+cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,
+                            cudaStream_t st);
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st);
