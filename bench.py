@@ -233,6 +233,42 @@ def run_reference(args, dist):
     print(json.dumps(line), flush=True)
 
 
+def reference_cuda_compare(args, fs):
+    """Time NCCA/libfluid's own device code (compiled unmodified from its
+    sources, driven by oracle/ref_runner.cu) and this library on the same
+    1M-particle scene in the reference's unit cube (res 100, h = 0.01 m)."""
+    from oracle import ref_cuda
+    if not ref_cuda.available():
+        return {"unavailable": "oracle/_ref/libfluid_ref.cubin not built (needs the reference sources)"}
+    spec, desc = workload("dam_break_1m_cube")
+    pos, vel = spec.positions(), spec.velocities()
+    p = spec.params()
+    rp = dict(p)
+    rp["gx"], rp["gy"], rp["gz"] = p["gravity"]
+    k = max(10, min(args.steps, 200))
+    try:
+        t = ref_cuda.time_steps(pos, vel, spec.unit_cube_res, spec.dt, rp, warmup=3, steps=k)
+    except Exception as e:  # the reference's failure is reported, not raised
+        return {"unavailable": f"reference runner failed: {str(e)[:200]}"}
+    ref_rate = spec.n * t["steps"] / (t["ms"] * 1e-3)
+    configure(fs, spec, pos, vel)
+    for _ in range(3):
+        fs.advance(spec.dt, 1)
+    fs.sync()
+    fs.timerMark(2)
+    for _ in range(k):
+        fs.advanceAsync(spec.dt, 1)
+    fs.timerMark(3)
+    ms = fs.timerElapsed(2, 3)
+    fs.sync()
+    ours = spec.n * k / (ms * 1e-3)
+    return {"workload": desc, "steps": k, "value": ref_rate, "unit": "particle-steps/s",
+            "ms_per_step": t["ms"] / t["steps"], "ours_value": ours, "ours_ms_per_step": ms / k,
+            "speedup": ours / ref_rate,
+            "how": "reference cudasrc kernels + thrust hash/sort/scan/reduce, its 4 syncs and blocking reduce per "
+                   "substep (oracle/ref_runner.cu); CUDA events around both loops after 3 warm-up substeps"}
+
+
 def run_ours(args, dist):
     from libfluid_gb300 import FluidSystem, _capi
     spec, desc = workload(args.workload)
@@ -323,6 +359,11 @@ def run_ours(args, dist):
         cpu = {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                "sample": f"{steps} substeps of the same {n}-particle scene on the host, {secs:.1f} s"}
 
+    # ---- the reference's own CUDA step on its unit-cube domain, beside ours ----
+    refcuda = None
+    if not args.skip_refcuda and dist.world == 1:
+        refcuda = reference_cuda_compare(args, fs)
+
     # hash, 3 scan kernels, scatter, rank+gather, density, force+integrate,
     # xsph (+ normals with surface tension); the count memset is not a kernel
     launches_per_substep = 9 + (1 if spec.surface_tension != 0.0 else 0)
@@ -334,12 +375,153 @@ def run_ours(args, dist):
                              ((n * 160 + cells * 8) / 1e6),
                        "parallelism": "replicas" if dist.world > 1 else "single GPU",
                        "timing": "CUDA events on the library stream, graph replay"},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "reference_cuda": refcuda,
             "gpu_launches": launches_per_substep * args.steps, "clocks": clk,
             "passes_ms_per_substep": per_launch,
             "published_reference": {"value": 7.7e7, "unit": "particle-steps/s",
                                     "note": "README: 1M particles at 77 FPS on an RTX 2080; grid, dt and substeps "
                                             "unstated, so not the same configuration"}}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_batched(args, dist):
+    """256 mixed-size dam breaks (2,048-65,536 particles each) advanced by one
+    launch per pass, against the plain step run one scene at a time."""
+    from libfluid_gb300 import workloads as W
+    from libfluid_gb300.batch import Batch
+    specs = W.batch_manifest(num_scenes=args.scenes, seed=7)
+    b = Batch(dist.local)
+    for s in specs:
+        b.add_scene(s)
+    total_n = sum(s.n for s in specs)
+    for _ in range(args.warmup):
+        b.step(1)
+    clocks = ClockSampler(dist.local)
+    clocks.start()
+    b.sync()
+    b.timer_mark(0)
+    for _ in range(args.steps):
+        b.step_async(1)
+    b.timer_mark(1)
+    ms = b.timer_elapsed(0, 1)
+    b.sync()
+    clk = clocks.stop()
+    value = total_n * args.steps / (ms * 1e-3)
+    b.close()
+    # plain step, one scene at a time (each scene its own engine, graph replay)
+    k_plain = max(3, min(args.steps, 50))
+    plain_ms = 0.0
+    for s in specs:
+        one = Batch(dist.local)
+        one.add_scene(s)
+        for _ in range(3):
+            one.step(1)
+        one.sync()
+        one.timer_mark(0)
+        for _ in range(k_plain):
+            one.step_async(1)
+        one.timer_mark(1)
+        plain_ms += one.timer_elapsed(0, 1)
+        one.close()
+    plain = total_n * k_plain / (plain_ms * 1e-3)
+    line = {"metric": METRIC, "workload": "batched", "value": value, "unit": "particle-steps/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(specs)} dam-break scenes, particles log-uniform [2048, 65536], aspect "
+                                   "[0.5,2], box 2x/1.2x the block, visc U[0.005,0.05], tension U[0,0.07], "
+                                   "spacing 0.01 m, h 0.02 m, dt 2e-4 s", "scenes": len(specs),
+                       "particles": total_n, "timing": "CUDA events, graph replay, one launch per pass"},
+            "plain_one_at_a_time": {"value": plain, "steps": k_plain,
+                                    "how": "each scene alone in its own engine, graph replay, summed device time"},
+            "speedup_vs_plain": value / plain, "clocks": clk}
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def served_requests(count: int, seed: int):
+    """Requests of the served workload: dam breaks as in the batched set but
+    with particles log-uniform in [1,024, 262,144] and substeps uniform in
+    [50, 500]."""
+    from libfluid_gb300 import workloads as W
+    specs = W.batch_manifest(num_scenes=count, seed=seed, nmin=1024, nmax=262144)
+    rng = np.random.default_rng(seed + 1)
+    steps = rng.integers(50, 501, size=count)
+    return specs, [int(x) for x in steps]
+
+
+def run_served(args, dist):
+    """Open-loop Poisson arrivals at each rate of --rates; p50/p99 latency
+    (arrival to final state on the host) and aggregate particle-steps/s,
+    against the plain sequential step on the same requests."""
+    import threading
+    from libfluid_gb300.batch import Batch
+    from libfluid_gb300.server import Server
+    specs, steps = served_requests(args.requests, seed=13)
+    work = sum(s.n * k for s, k in zip(specs, steps))
+    # plain sequential step: per-substep device time of each request alone
+    # (graph replay), summed over its substeps
+    plain_ms = 0.0
+    sample = list(range(0, len(specs), max(1, len(specs) // 64)))
+    sample_work = 0
+    for i in sample:
+        one = Batch(dist.local)
+        one.add_scene(specs[i])
+        for _ in range(3):
+            one.step(1)
+        one.sync()
+        one.timer_mark(0)
+        for _ in range(20):
+            one.step_async(1)
+        one.timer_mark(1)
+        plain_ms += one.timer_elapsed(0, 1) / 20 * steps[i]
+        sample_work += specs[i].n * steps[i]
+        one.close()
+    plain_rate = sample_work / (plain_ms * 1e-3)
+    results = []
+    rng = np.random.default_rng(99)
+    for rate in args.rates:
+        srv = Server(dist.local, memory_budget=100 << 30)
+        gaps = rng.exponential(1.0 / rate, size=len(specs))
+        ids = [None] * len(specs)
+        t0 = time.perf_counter()
+
+        def producer():
+            t = t0
+            for i, (s, k) in enumerate(zip(specs, steps)):
+                t += gaps[i]
+                d = t - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                ids[i] = srv.submit(s, k)
+
+        th = threading.Thread(target=producer)
+        th.start()
+        th.join()
+        srv.drain(-1)
+        wall = time.perf_counter() - t0
+        lat = []
+        first, last = 1e30, 0.0
+        for rid in ids:
+            ts, ta, td = srv.times(rid)
+            lat.append(td - ts)
+            first, last = min(first, ts), max(last, td)
+        st = srv.stats()
+        srv.close()
+        lat = np.asarray(lat)
+        results.append({"rate_req_s": rate, "requests": len(specs), "p50_s": float(np.percentile(lat, 50)),
+                        "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+                        "throughput": work / (last - first), "wall_s": wall,
+                        "busy_frac": st["busy_seconds"] / max(last - first, 1e-9),
+                        "mean_live_scenes": None, "peak_live_particles": st["peak_live_particles"]})
+    line = {"metric": METRIC, "workload": "served", "unit": "particle-steps/s", "value": max(r["throughput"] for r in results),
+            "higher_is_better": True, "n_gpus": dist.world, "dtype": "f32", "data": "synthetic",
+            "config": {"requests": len(specs), "particles": "log-uniform [1024, 262144]", "substeps": "U[50,500]",
+                       "arrivals": "open-loop Poisson", "memory_budget_bytes": 100 << 30,
+                       "offered_particle_steps": work},
+            "plain_sequential": {"value": plain_rate, "how": f"{len(sample)} requests alone, per-substep device "
+                                                             "time x their substeps"},
+            "rates": results}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -353,11 +535,20 @@ def main():
     ap.add_argument("--workload", default="dam_break_1m")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-refcuda", action="store_true")
+    ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
+    ap.add_argument("--requests", type=int, default=1000, help="served workload: number of requests")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000],
+                    help="served workload: Poisson arrival rates (req/s)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     dist = Dist()
     if args.impl == "reference":
         run_reference(args, dist)
+    elif args.workload == "batched":
+        run_batched(args, dist)
+    elif args.workload == "served":
+        run_served(args, dist)
     else:
         run_ours(args, dist)
 

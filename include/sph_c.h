@@ -83,6 +83,12 @@ int64_t sph_substep_count(float full_dt, uint32_t substeps);
  * colour (DensityColourOperator, fluidutil.cu:67-80) and velocities in the
  * order of the last substep's cell sort.  Any pointer may be NULL. */
 int sph_export(sph_system* s, float* pos, float* colour, float* vel, uint32_t n);
+/* Houdini PGEOMETRY V5 export of one frame, byte-identical to fluidtest's
+ * dumpToGeo (test/src/main.cpp:10-74): pos/colour/vel packed xyz, n points.
+ * sph_geo_path formats "<filebase>.<frame:04d>.geo" (test/src/main.cpp:17-18). */
+int sph_write_geo(const char* path, const float* pos, const float* colour, const float* vel, uint32_t n,
+                  float pscale);
+int sph_geo_path(char* out, uint64_t cap, const char* filebase, uint32_t frame);
 /* FluidSystem::getPscale (fluidsystem.cu:406-409) */
 int sph_get_pscale(const sph_system* s, float* out);
 uint32_t sph_num_particles(const sph_system* s);
@@ -145,13 +151,27 @@ enum sph_field {
     SPH_FIELD_FVISCOSITY = 11,/* f32[3n] viscosity force (needs debug taps) */
     SPH_FIELD_NORMAL = 12,    /* f32[3n] m_Normals (surface tension scenes only) */
     SPH_FIELD_POS_SORTED = 13,/* f32[3n] positions in cell order before integration */
-    SPH_FIELD_ACC = 14        /* f32[3n] m_Acceleration */
+    SPH_FIELD_ACC = 14,       /* f32[3n] m_Acceleration */
+    SPH_FIELD_VEL_INT = 15    /* f32[3n] velocity after integration, before XSPH */
 };
 /* Enable the optional taps (neighbour counts, force components). */
 int sph_debug_enable(sph_system* s, int on);
 int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
 
 /* ---- execution options and profiling ----------------------------------- */
+/* How the substep is launched (no effect on results: every choice computes
+ * the same values bit for bit).  tile: particles per tile = threads per
+ * block (64, 128 or 256); persistent: 0 = one block per tile, k > 0 = k
+ * blocks per SM taking tiles from a counter in the neighbour passes; skin:
+ * neighbour-mask skin in units of h, in (0, 1]. */
+typedef struct sph_exec_config {
+    uint32_t tile;
+    uint32_t persistent;
+    float skin;
+    uint32_t pad_;
+} sph_exec_config;
+int sph_set_exec(sph_system* s, const sph_exec_config* e);
+int sph_get_exec(const sph_system* s, sph_exec_config* e);
 int sph_set_use_graph(sph_system* s, int on);     /* CUDA-graph replay of the substep (default on) */
 int sph_set_profiling(sph_system* s, int on);     /* per-pass CUDA events (disables the graph) */
 /* Accumulated per-pass milliseconds since profiling was enabled, in the
@@ -168,6 +188,106 @@ int sph_timer_mark(sph_system* s, int slot);
 int sph_timer_elapsed(sph_system* s, int a, int b, float* ms);
 const char* sph_last_error(const sph_system* s);
 const char* sph_version(void);
+
+/* ---- batched step -------------------------------------------------------
+ * Many independent scenes (each a FluidSystem with its own domain, parameters
+ * and particle count) advanced together: every pass of the substep is one
+ * launch over all live scenes (segmented hash and sort with per-scene cell
+ * ranges, scene-aware neighbour kernels), and the whole substep is replayed
+ * as one CUDA graph.  No counterpart in the reference, which holds one
+ * parameter block per process (fluidparams.cu:6) and so one system at a time. */
+typedef struct sph_batch sph_batch;
+typedef struct sph_lattice {
+    float lo[3];            /* block corner */
+    float spacing;          /* lattice spacing */
+    uint32_t nx, ny, nz;    /* sites per axis; particle (ix*ny+iy)*nz+iz */
+    float jitter;           /* uniform jitter amplitude (+/-), seeded */
+    float vel[3];           /* initial velocity */
+    uint32_t pad_;
+    uint64_t seed;
+} sph_lattice;
+int sph_batch_create(sph_batch** out, int device);
+int sph_batch_destroy(sph_batch* b);
+/* Add a scene of n particles with parameters p (p->dt is its substep dt);
+ * state starts at zero.  Returns its id in *scene_id. */
+int sph_batch_add_scene(sph_batch* b, const sph_params* p, uint32_t n, int* scene_id);
+int sph_batch_remove_scene(sph_batch* b, int scene_id);
+int sph_batch_set_params(sph_batch* b, int scene_id, const sph_params* p);
+int sph_batch_set_state(sph_batch* b, int scene_id, const float* pos, const float* vel, uint32_t n);
+/* Fill particles [first, first + nx*ny*nz) of a scene with a jittered
+ * lattice block generated on the device. */
+int sph_batch_generate_lattice(sph_batch* b, int scene_id, const sph_lattice* spec, uint32_t first);
+/* Advance every live scene by `substeps` substeps of its own dt (blocking). */
+int sph_batch_step(sph_batch* b, uint32_t substeps);
+int sph_batch_step_async(sph_batch* b, uint32_t substeps);
+int sph_batch_sync(sph_batch* b);
+int sph_batch_get_state(sph_batch* b, int scene_id, float* pos, float* colour, float* vel, uint32_t n);
+uint32_t sph_batch_num_scenes(const sph_batch* b);
+uint64_t sph_batch_num_particles(const sph_batch* b);
+int sph_batch_debug_enable(sph_batch* b, int on);
+int sph_batch_debug_get(sph_batch* b, int scene_id, int field, void* buf, uint64_t count);
+int sph_batch_set_use_graph(sph_batch* b, int on);
+int sph_batch_set_exec(sph_batch* b, const sph_exec_config* e);
+int sph_batch_timer_mark(sph_batch* b, int slot);
+int sph_batch_timer_elapsed(sph_batch* b, int a, int b2, float* ms);
+const char* sph_batch_last_error(const sph_batch* b);
+
+/* ---- served step (continuous batching) ----------------------------------
+ * A request loop on its own host thread.  Requests (a scene: parameters,
+ * initial state, number of substeps) are queued as they arrive and admitted
+ * in arrival order while the device-memory budget and the live-scene limit
+ * allow; admitted scenes stay resident on the GPU and every loop iteration
+ * advances all live scenes by one substep in one batched step; a scene that
+ * has run its substeps is copied to the host and leaves, freeing memory for
+ * the queue.  No counterpart in the reference. */
+typedef struct sph_server sph_server;
+typedef struct sph_server_config {
+    int device;                 /* CUDA device, -1 = current */
+    uint64_t memory_budget;     /* device bytes the scenes may occupy */
+    uint32_t max_live_scenes;   /* 0 = no limit */
+    uint32_t substeps_per_iteration; /* substeps between admissions (>= 1) */
+} sph_server_config;
+typedef struct sph_request {
+    sph_params params;          /* domain and physics; params.dt is the substep */
+    uint32_t n;                 /* particles */
+    uint32_t steps;             /* substeps to run */
+    const float* pos;           /* initial positions (host, packed xyz), or NULL to use blocks */
+    const float* vel;           /* initial velocities, or NULL for zero */
+    const sph_lattice* blocks;  /* lattice blocks generated on the device (when pos == NULL) */
+    uint32_t num_blocks;
+    uint32_t pad_;
+} sph_request;
+enum sph_request_state { SPH_REQ_QUEUED = 0, SPH_REQ_RUNNING = 1, SPH_REQ_DONE = 2, SPH_REQ_FAILED = 3,
+                         SPH_REQ_UNKNOWN = 4 };
+typedef struct sph_server_stats {
+    uint64_t submitted, admitted, completed, failed, rejected;
+    uint64_t iterations;        /* batched steps run */
+    uint64_t particle_steps;    /* sum over completed and live scenes */
+    double busy_seconds;        /* time spent stepping */
+    uint32_t live_scenes, queued;
+    uint64_t live_particles;
+    uint64_t device_bytes;      /* arena footprint */
+    uint64_t peak_live_particles;
+} sph_server_stats;
+int sph_server_create(sph_server** out, const sph_server_config* cfg);
+/* Stops the loop (running scenes are abandoned) and frees everything. */
+int sph_server_destroy(sph_server* s);
+/* Queue a request; the input arrays are copied.  SPH_EBUSY if it can never
+ * fit the memory budget. */
+int sph_server_submit(sph_server* s, const sph_request* req, uint64_t* request_id);
+int sph_server_state(sph_server* s, uint64_t request_id);
+/* Wait until the request is done or failed, at most timeout_ms (< 0: no
+ * limit); SPH_ETIMEOUT if it is still pending. */
+int sph_server_wait(sph_server* s, uint64_t request_id, int64_t timeout_ms);
+/* Copy a finished request's final positions and velocities (either may be
+ * NULL) and release it. */
+int sph_server_fetch(sph_server* s, uint64_t request_id, float* pos, float* vel, uint32_t n);
+/* Seconds since server start at submission, admission and completion. */
+int sph_server_times(sph_server* s, uint64_t request_id, double* t_submit, double* t_admit, double* t_done);
+int sph_server_get_stats(sph_server* s, sph_server_stats* out);
+/* Block until the queue is empty and no scene is live (or timeout). */
+int sph_server_drain(sph_server* s, int64_t timeout_ms);
+const char* sph_server_last_error(sph_server* s);
 
 /* ---- allocation-free cell-start scan ------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

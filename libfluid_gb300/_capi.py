@@ -18,7 +18,7 @@ STATUS_NAMES = {0: "SPH_OK", 1: "SPH_EINVAL", 2: "SPH_ENOMEM", 3: "SPH_ECUDA", 4
 FIELDS = {
     "hash": 0, "perm": 1, "cellstart": 2, "cellocc": 3, "nbrcount": 4, "density": 5, "pressure": 6,
     "soundspeed": 7, "fpressure": 8, "ftension": 9, "fadhesion": 10, "fviscosity": 11, "normal": 12,
-    "pos_sorted": 13, "acc": 14,
+    "pos_sorted": 13, "acc": 14, "vel_int": 15,
 }
 
 
@@ -29,6 +29,10 @@ class SphParams(C.Structure):
                 ("surface_tension", C.c_float), ("viscosity", C.c_float), ("adhesion", C.c_float),
                 ("vdamp", C.c_float), ("vel_limit", C.c_float), ("acc_limit", C.c_float), ("dt", C.c_float),
                 ("gravity", C.c_float * 3)]
+
+
+class SphExec(C.Structure):
+    _fields_ = [("tile", C.c_uint32), ("persistent", C.c_uint32), ("skin", C.c_float), ("pad_", C.c_uint32)]
 
 
 class SphError(RuntimeError):
@@ -83,6 +87,8 @@ SIGNATURES = [
     ("sph_debug_get", _I, [_P, _I, _P, C.c_uint64]),
     ("sph_set_use_graph", _I, [_P, _I]),
     ("sph_set_profiling", _I, [_P, _I]),
+    ("sph_set_exec", _I, [_P, C.POINTER(SphExec)]),
+    ("sph_get_exec", _I, [_P, C.POINTER(SphExec)]),
     ("sph_get_pass_times", _I, [_P, C.POINTER(C.c_double), _I, C.POINTER(C.c_uint64)]),
     ("sph_pass_name", C.c_char_p, [_I]),
     ("sph_host_register", _I, [_P, C.c_uint64]),
@@ -92,6 +98,8 @@ SIGNATURES = [
     ("sph_last_error", C.c_char_p, [_P]),
     ("sph_version", C.c_char_p, []),
     ("sph_scan_cells_noalloc", _I, [_P, _U32, _P, _P]),
+    ("sph_write_geo", _I, [C.c_char_p, _P, _P, _P, _U32, _F]),
+    ("sph_geo_path", _I, [C.c_char_p, C.c_uint64, C.c_char_p, _U32]),
 ]
 
 

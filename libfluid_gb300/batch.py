@@ -1,0 +1,145 @@
+"""Python host mirror of the batched step (include/sph_c.h, sph_batch_*)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._capi import SphParams, check, lib
+from ._capi_batch import SphLattice
+from .workloads import Lattice, SceneSpec
+
+
+def params_struct(spec: SceneSpec) -> SphParams:
+    p = SphParams()
+    if spec.unit_cube_res:
+        p.box_mode, p.res = 0, spec.unit_cube_res
+        p.lx = p.ly = p.lz = 1.0
+        p.h = 1.0 / spec.unit_cube_res
+    else:
+        p.box_mode, p.res = 1, 0
+        p.lx, p.ly, p.lz = spec.box
+        p.h = spec.h
+    d = spec.params()
+    for k in ("rest_density", "gas_constant", "gamma", "mass", "particle_size", "xsph", "surface_tension",
+              "viscosity", "adhesion", "vdamp", "vel_limit", "acc_limit", "dt"):
+        setattr(p, k, float(d[k]))
+    for i in range(3):
+        p.gravity[i] = float(d["gravity"][i])
+    return p
+
+
+def lattice_struct(b: Lattice) -> SphLattice:
+    s = SphLattice()
+    for i in range(3):
+        s.lo[i] = float(b.lo[i])
+        s.vel[i] = float(b.vel[i])
+    s.spacing, s.jitter = float(b.spacing), float(b.jitter)
+    s.nx, s.ny, s.nz = b.nx, b.ny, b.nz
+    s.seed = int(b.seed)
+    return s
+
+
+class Batch:
+    """Many independent scenes advanced with one launch per pass."""
+
+    def __init__(self, device: int = -1):
+        self._L = lib()
+        h = C.c_void_p()
+        check(self._L.sph_batch_create(C.byref(h), device))
+        self._h = h
+        self.scenes: dict[int, SceneSpec] = {}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.sph_batch_destroy(h)
+            self._h = None
+
+    def close(self):
+        self.__del__()
+
+    def _ck(self, code):
+        if code != 0:
+            raw = self._L.sph_batch_last_error(self._h)
+            from ._capi import SphError
+            raise SphError(code, raw.decode() if raw else "")
+
+    def add_scene(self, spec: SceneSpec, generate: bool = True) -> int:
+        sid = C.c_int(-1)
+        p = params_struct(spec)
+        self._ck(self._L.sph_batch_add_scene(self._h, C.byref(p), spec.n, C.byref(sid)))
+        self.scenes[sid.value] = spec
+        if generate:
+            first = 0
+            for b in spec.blocks:
+                s = lattice_struct(b)
+                self._ck(self._L.sph_batch_generate_lattice(self._h, sid.value, C.byref(s), first))
+                first += b.n
+        return sid.value
+
+    def remove_scene(self, sid: int) -> None:
+        self._ck(self._L.sph_batch_remove_scene(self._h, sid))
+        self.scenes.pop(sid, None)
+
+    def set_state(self, sid: int, pos, vel=None) -> None:
+        p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+        v = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        self._ck(self._L.sph_batch_set_state(self._h, sid, p.ctypes.data, None if v is None else v.ctypes.data,
+                                             p.shape[0]))
+
+    def step(self, substeps: int = 1) -> None:
+        self._ck(self._L.sph_batch_step(self._h, substeps))
+
+    def step_async(self, substeps: int = 1) -> None:
+        self._ck(self._L.sph_batch_step_async(self._h, substeps))
+
+    def sync(self) -> None:
+        self._ck(self._L.sph_batch_sync(self._h))
+
+    def get_state(self, sid: int):
+        n = self.scenes[sid].n
+        outs = [np.empty((n, 3), np.float32) for _ in range(3)]
+        self._ck(self._L.sph_batch_get_state(self._h, sid, *[o.ctypes.data for o in outs], n))
+        return tuple(outs)
+
+    @property
+    def num_scenes(self) -> int:
+        return int(self._L.sph_batch_num_scenes(self._h))
+
+    @property
+    def num_particles(self) -> int:
+        return int(self._L.sph_batch_num_particles(self._h))
+
+    def debug_enable(self, on: bool = True) -> None:
+        self._ck(self._L.sph_batch_debug_enable(self._h, 1 if on else 0))
+
+    def debug(self, sid: int, field: str, ncells: int | None = None) -> np.ndarray:
+        from ._capi import FIELDS
+        n = self.scenes[sid].n
+        if field in ("cellstart", "cellocc"):
+            out = np.empty(int(ncells), np.uint32)
+        elif field in ("hash", "perm", "nbrcount"):
+            out = np.empty(n, np.uint32)
+        elif field in ("density", "pressure", "soundspeed"):
+            out = np.empty(n, np.float32)
+        else:
+            out = np.empty((n, 3), np.float32)
+        self._ck(self._L.sph_batch_debug_get(self._h, sid, FIELDS[field], out.ctypes.data, out.size))
+        return out
+
+    def set_use_graph(self, on: bool) -> None:
+        self._ck(self._L.sph_batch_set_use_graph(self._h, 1 if on else 0))
+
+    def set_exec(self, tile: int = 256, persistent: int = 0, skin: float = 0.2) -> None:
+        from ._capi import SphExec
+        e = SphExec(tile, persistent, skin, 0)
+        self._ck(self._L.sph_batch_set_exec(self._h, C.byref(e)))
+
+    def timer_mark(self, slot: int) -> None:
+        self._ck(self._L.sph_batch_timer_mark(self._h, slot))
+
+    def timer_elapsed(self, a: int, b: int) -> float:
+        ms = C.c_float(0.0)
+        self._ck(self._L.sph_batch_timer_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value

@@ -46,7 +46,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", f"-I{IN
              f"-I{os.path.join(CUDA, 'include')}"]
 
 KERNEL_SOURCES = ["sph_kernels.cu", "sph_noalloc.cu"]
-HOST_SOURCES = ["engine.cpp", "capi.cpp"]
+HOST_SOURCES = ["engine.cpp", "capi.cpp", "capi_batch.cpp", "server.cpp", "geo.cpp"]
 
 LIB_SPH = os.path.join(PKG, "libsph_gb300.so")
 LIB_FLUID = os.path.join(PKG, "libfluid.so")
@@ -118,9 +118,36 @@ def build(force: bool = False, verbose: bool = False) -> dict:
     if os.path.exists(drv_src) and (force or not _newer(drv, [drv_src, LIB_FLUID] + hdrs)):
         _run([CXX] + CXX_FLAGS + [drv_src, "-o", drv, f"-L{PKG}", "-lfluid", "-lsph_gb300",
                                   "-Wl,-rpath,$ORIGIN/.."])
+    build_reference_runner(force=force)
     if verbose:
         print(f"built {LIB_SPH}, {LIB_ORACLE}")
     return {"sph": LIB_SPH, "fluid": LIB_FLUID, "oracle": LIB_ORACLE}
+
+
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
+REF_CUBIN = os.path.join(REF_DIR, "libfluid_ref.cubin")
+REF_RUNNER = os.path.join(REF_DIR, "ref_runner")
+
+
+def build_reference_runner(force: bool = False) -> bool:
+    """Oracle pins: the reference's own device code as a cubin (built only
+    where the reference tree is present, by oracle/ref_build.sh) and the host
+    runner that drives it (oracle/ref_runner.cu, built wherever the cubin
+    is).  Test infrastructure; returns False when the cubin is unavailable."""
+    script = os.path.join(ROOT, "oracle", "ref_build.sh")
+    deps = [os.path.join(ROOT, "oracle", "ref_unity.cu"), os.path.join(ROOT, "oracle", "ref_compat", "helper_math.h"),
+            script]
+    if force or not _newer(REF_CUBIN, deps):
+        r = subprocess.run(["bash", script], capture_output=True, text=True)
+        if r.returncode not in (0, 2):
+            raise RuntimeError("reference device build failed:\n" + r.stdout + r.stderr)
+    if not os.path.exists(REF_CUBIN):
+        return False
+    src = os.path.join(ROOT, "oracle", "ref_runner.cu")
+    if force or not _newer(REF_RUNNER, [src]):
+        _run([NVCC, "-O2", "-std=c++17"] + GENCODE + [src, "-o", REF_RUNNER,
+                                                      f"-L{os.path.join(CUDA, 'lib64', 'stubs')}", "-lcuda"])
+    return True
 
 
 if __name__ == "__main__":

@@ -351,6 +351,23 @@ int sph_set_use_graph(sph_system* s, int on) {
     s->eng->set_use_graph(on != 0);
     return SPH_OK;
 }
+int sph_set_exec(sph_system* s, const sph_exec_config* e) {
+    if (!s || !e) return SPH_EINVAL;
+    sph::ExecConfig x;
+    x.tile = e->tile;
+    x.persistent = e->persistent;
+    x.skin = e->skin;
+    return eng_err(s, s->eng->set_exec(x));
+}
+int sph_get_exec(const sph_system* s, sph_exec_config* e) {
+    if (!s || !e) return SPH_EINVAL;
+    const sph::ExecConfig& x = s->eng->exec();
+    e->tile = x.tile;
+    e->persistent = x.persistent;
+    e->skin = x.skin;
+    e->pad_ = 0;
+    return SPH_OK;
+}
 int sph_set_profiling(sph_system* s, int on) {
     if (!s) return SPH_EINVAL;
     return eng_err(s, s->eng->set_profiling(on != 0));

@@ -87,10 +87,15 @@ bool derive_params(const SceneConfig& c, DevParams& d, std::string* err) {
     d.grav_x = c.gravity[0]; d.grav_y = c.gravity[1]; d.grav_z = c.gravity[2];
     d.eps = FLT_MIN;
     d.flags = (c.surface_tension != 0.0f) ? 1u : 0u;
+    const float skin = (c.skin > 0.0f) ? c.skin : SPH_SKIN_DEFAULT;
+    const float rs = (1.0f + skin) * h;
+    d.skin2 = rs * rs;
+    d.inv_h2 = 1.0f / d.h2;
+    d.xsph_disp_limit2 = 0.25f * skin * skin * 0.98f;
     return true;
 }
 
-uint64_t Engine::bytes_per_particle() { return 9 * 16 + 4 * 4; }
+uint64_t Engine::bytes_per_particle() { return 9 * 16 + 4 * 4 + 9 * 4; }
 uint64_t Engine::bytes_per_cell() { return 2 * 4 + 1; }
 const char* Engine::pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : "?"; }
 
@@ -102,6 +107,8 @@ Engine::Engine(int device) {
     cudaMallocHost((void**)&h_status_, sizeof(uint32_t));
     cudaMalloc((void**)&status_, sizeof(uint32_t));
     cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_);
+    cudaMalloc((void**)&scal_, 8 * sizeof(uint32_t));
+    cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_);
     for (auto& e : ev_) cudaEventCreate(&e);
 }
 
@@ -114,6 +121,7 @@ Engine::~Engine() {
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     for (auto& e : timers_) if (e) cudaEventDestroy(e);
     if (status_) cudaFree(status_);
+    if (scal_) cudaFree(scal_);
     if (h_status_) cudaFreeHost(h_status_);
     if (h_params_) cudaFreeHost(h_params_);
     if (stream_) cudaStreamDestroy(stream_);
@@ -136,7 +144,7 @@ int Engine::cuda_fail(cudaError_t e, const char* what) {
 void Engine::free_all() {
     float4** f4[] = {&P0_, &P1_, &V0_, &V1_, &V2_, &A0_, &A1_, &S_, &N_, &dbg_forces_};
     for (auto p : f4) { if (*p) cudaFree(*p); *p = nullptr; }
-    uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &count_, &start_, &scan_sums_, &dbg_nbr_};
+    uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &count_, &start_, &scan_sums_, &dbg_nbr_, &mask_};
     for (auto p : u) { if (*p) cudaFree(*p); *p = nullptr; }
     if (stage_) cudaFree(stage_);
     stage_ = nullptr;
@@ -152,8 +160,13 @@ void Engine::free_all() {
 // Grow the particle and cell arenas, preserving live particle state.
 int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
     cudaSetDevice(device_);
+    if (byte_limit_) {
+        const uint64_t need = std::max(parts, pcap_) * bytes_per_particle() + std::max(cells, ccap_) * 8;
+        if (need > byte_limit_) return fail(ENG_ENOMEM, "arena would exceed the memory budget");
+    }
     if (parts > pcap_) {
-        const uint64_t np = std::max<uint64_t>(parts, pcap_ + pcap_ / 2);
+        uint64_t np = std::max<uint64_t>(parts, pcap_ + pcap_ / 2);
+        if (byte_limit_ && np * bytes_per_particle() + std::max(cells, ccap_) * 8 > byte_limit_) np = parts;
         if (np >= (1ull << 31)) return fail(ENG_ENOMEM, "particle capacity exceeds 2^31");
         float4** state[] = {&P0_, &V0_, &A0_, &S_};
         float4** scratch[] = {&P1_, &V1_, &V2_, &A1_, &N_};
@@ -181,6 +194,12 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
             cudaError_t e = cudaMalloc((void**)p, np * sizeof(uint32_t));
             if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
         }
+        if (mask_) cudaFree(mask_);
+        mask_ = nullptr;
+        {
+            cudaError_t e = cudaMalloc((void**)&mask_, 9 * np * sizeof(uint32_t));
+            if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+        }
         if (dbg_nbr_) { cudaFree(dbg_nbr_); dbg_nbr_ = nullptr; }
         if (dbg_forces_) { cudaFree(dbg_forces_); dbg_forces_ = nullptr; }
         if (debug_) {
@@ -191,7 +210,8 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
         graph_dirty_ = true;
     }
     if (cells > ccap_) {
-        const uint64_t nc = std::max<uint64_t>(cells, ccap_ + ccap_ / 2);
+        uint64_t nc = std::max<uint64_t>(cells, ccap_ + ccap_ / 2);
+        if (byte_limit_ && pcap_ * bytes_per_particle() + nc * 8 > byte_limit_) nc = cells;
         if (count_) cudaFree(count_);
         if (start_) cudaFree(start_);
         if (scan_sums_) cudaFree(scan_sums_);
@@ -269,9 +289,26 @@ const Scene* Engine::scene(int id) const {
     return nullptr;
 }
 
-int Engine::add_scene(const SceneConfig& cfg, uint32_t n, int* id_out) {
+int Engine::set_exec(const ExecConfig& e) {
+    if (e.tile != 64 && e.tile != 128 && e.tile != 256) return fail(ENG_EINVAL, "tile must be 64, 128 or 256");
+    if (!(e.skin > 0.0f && e.skin <= 1.0f)) return fail(ENG_EINVAL, "skin must be in (0, 1]");
+    if (e.persistent > 64) return fail(ENG_EINVAL, "persistent blocks per SM must be <= 64");
+    if (e.tile != exec_.tile) layout_dirty_ = true;
+    graph_dirty_ = true;
+    exec_ = e;
+    for (auto& s : scenes_) {
+        s.cfg.skin = e.skin;
+        derive_params(s.cfg, s.dp, nullptr);
+    }
+    params_dirty_ = true;
+    return ENG_OK;
+}
+
+int Engine::add_scene(const SceneConfig& cfg_in, uint32_t n, int* id_out) {
     Scene s;
     std::string e;
+    SceneConfig cfg = cfg_in;
+    cfg.skin = exec_.skin;
     if (!derive_params(cfg, s.dp, &e)) return fail(ENG_EINVAL, e);
     if (n == 0) return fail(ENG_EINVAL, "a scene needs at least one particle");
     s.cfg = cfg;
@@ -301,7 +338,9 @@ int Engine::remove_scene(int id) {
     return fail(ENG_EINVAL, "unknown scene id");
 }
 
-int Engine::set_config(int id, const SceneConfig& cfg) {
+int Engine::set_config(int id, const SceneConfig& cfg_in) {
+    SceneConfig cfg = cfg_in;
+    cfg.skin = exec_.skin;
     for (auto& s : scenes_) {
         if (s.id != id) continue;
         DevParams dp;
@@ -335,8 +374,9 @@ int Engine::rebuild_layout() {
         cell_base_[k] = (uint32_t)cb;
         h_scenes_[k] = DevScene{s.part_base, s.n, (uint32_t)cb, s.dp.ncells};
         cb += s.dp.ncells + 1ull;
-        for (uint32_t f = 0; f < s.n; f += SPH_TILE)
-            h_tiles_.push_back(make_uint4((uint32_t)k, s.part_base + f, std::min<uint32_t>(SPH_TILE, s.n - f), 0u));
+        const uint32_t tile = exec_.tile;
+        for (uint32_t f = 0; f < s.n; f += tile)
+            h_tiles_.push_back(make_uint4((uint32_t)k, s.part_base + f, std::min<uint32_t>(tile, s.n - f), 0u));
         any_tension_ = any_tension_ || (s.dp.flags & 1u);
     }
     total_cells_ = (uint32_t)cb;
@@ -391,6 +431,12 @@ StepArgs Engine::args() const {
     a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
     a.key = key_; a.slot = slot_; a.tmp = tmp_; a.perm = perm_;
     a.status = status_;
+    a.mask = mask_;
+    a.mask_stride = pcap_;
+    a.maxdisp = scal_;
+    a.block = exec_.tile;
+    a.tile_ctr = exec_.persistent ? scal_ + 4 : nullptr;
+    a.grid_nbr = exec_.persistent ? std::min<uint32_t>(a.ntiles, (uint32_t)sm_count_ * exec_.persistent) : a.ntiles;
     a.dbg_nbr = debug_ ? dbg_nbr_ : nullptr;
     a.dbg_forces = debug_ ? dbg_forces_ : nullptr;
     return a;
@@ -403,6 +449,7 @@ int Engine::launch_substep(bool profile) {
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     mark(0);
     ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), st), "memset counts");
+    ENG_CK(cudaMemsetAsync(scal_, 0, 8 * sizeof(uint32_t), st), "memset substep scalars");
     ENG_CK(launch_hash(a, st), "hash");
     mark(1);
     ENG_CK(launch_scan(a, st), "scan");
@@ -673,9 +720,10 @@ int Engine::debug_get(int id, int field, void* host, uint64_t count) {
         }
         case F_NORMAL:
         case F_POS_SORTED:
-        case F_ACC: {
+        case F_ACC:
+        case F_VEL_INT: {
             if (!need(3ull * n)) return fail(ENG_EINVAL, "buffer too small");
-            const float4* src = field == F_NORMAL ? N_ : field == F_POS_SORTED ? P1_ : A0_;
+            const float4* src = field == F_NORMAL ? N_ : field == F_POS_SORTED ? P1_ : field == F_ACC ? A0_ : V2_;
             std::vector<float4> v(n);
             ENG_CK(cudaMemcpy(v.data(), src + pb, n * sizeof(float4), cudaMemcpyDeviceToHost), "debug copy");
             float* out = (float*)host;

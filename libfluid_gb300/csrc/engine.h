@@ -22,6 +22,14 @@ struct SceneConfig {
     float xsph = 0.5f, surface_tension = 1.f, viscosity = 0.1f, adhesion = 1.f, vdamp = 1.f;
     float vel_limit = 5.f, acc_limit = 150.f, dt = 0.01f;
     float gravity[3] = {0.f, -9.8f, 0.f};
+    float skin = 0.f;                 // neighbour-mask skin in units of h (0: engine default)
+};
+
+// Execution choices of the substep (chosen by libfluid_gb300/autotune.py).
+struct ExecConfig {
+    uint32_t tile = 256;              // particles per tile = threads per block (64, 128 or 256)
+    uint32_t persistent = 0;          // 0: one block per tile; k > 0: k blocks per SM pull tiles
+    float skin = SPH_SKIN_DEFAULT;    // neighbour-mask skin (units of h)
 };
 
 // Derive the device parameter block (FluidParams::setRes and setters,
@@ -65,11 +73,14 @@ public:
     // Debug taps (copy to host).  Valid after at least one substep.
     int debug_enable(bool on);
     enum Field { F_HASH = 0, F_PERM, F_CELLSTART, F_CELLOCC, F_NBRCOUNT, F_DENSITY, F_PRESSURE, F_SOUNDSPEED,
-                 F_FPRESSURE, F_FTENSION, F_FADHESION, F_FVISCOSITY, F_NORMAL, F_POS_SORTED, F_ACC };
+                 F_FPRESSURE, F_FTENSION, F_FADHESION, F_FVISCOSITY, F_NORMAL, F_POS_SORTED, F_ACC, F_VEL_INT };
     int debug_get(int id, int field, void* host, uint64_t count);
 
     // Options.
     void set_use_graph(bool on) { use_graph_ = on; graph_dirty_ = true; }
+    int set_exec(const ExecConfig& e);
+    const ExecConfig& exec() const { return exec_; }
+    int sm_count() const { return sm_count_; }
     cudaStream_t stream() const { return stream_; }
     const std::string& last_error() const { return err_; }
     int device() const { return device_; }
@@ -88,6 +99,8 @@ public:
     static uint64_t bytes_per_particle();
     static uint64_t bytes_per_cell();
     uint64_t device_bytes() const { return dev_bytes_; }
+    // Cap on the arena footprint (0 = none): growth beyond it fails with ENG_ENOMEM.
+    void set_byte_limit(uint64_t bytes) { byte_limit_ = bytes; }
 
 private:
     int fail(int code, const std::string& msg);
@@ -116,6 +129,10 @@ private:
            *A1_ = nullptr, *S_ = nullptr, *N_ = nullptr;
     uint32_t *key_ = nullptr, *slot_ = nullptr, *tmp_ = nullptr, *perm_ = nullptr;
     uint32_t *count_ = nullptr, *start_ = nullptr, *scan_sums_ = nullptr, *status_ = nullptr;
+    uint32_t *mask_ = nullptr;        // 9 neighbour-mask words per slot
+    uint32_t *scal_ = nullptr;        // per-substep scalars: [0] displacement max, [4..7] tile counters
+    ExecConfig exec_;
+    int sm_count_ = 1;
     uint32_t* dbg_nbr_ = nullptr;
     float* stage_ = nullptr;           // device staging for packed xyz transfers
     size_t stage_bytes_ = 0;
@@ -125,6 +142,7 @@ private:
     uint4* d_tiles_ = nullptr;
     uint64_t scene_cap_ = 0, tile_cap_ = 0;
     uint64_t dev_bytes_ = 0;
+    uint64_t byte_limit_ = 0;
     // host mirrors
     DevParams* h_params_ = nullptr;    // pinned
     uint32_t* h_status_ = nullptr;     // pinned

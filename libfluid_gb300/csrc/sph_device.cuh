@@ -110,6 +110,71 @@ __device__ __forceinline__ void for_candidates(const DevParams& P, const uint32_
     }
 }
 
+// Row r (0..8) of the neighbourhood of grid cell g, dz = r/3-1, dy = r%3-1:
+// the slot range [jb, je) of cells (x-1..x+1, y+dy, z+dz) clipped at the
+// grid edge.  Returns false when the row lies outside the grid.  The rows are
+// visited in the same order by every pass, so a candidate's (row, offset)
+// names the same particle in the density, normal, force and XSPH passes.
+__device__ __forceinline__ bool row_range(const DevParams& P, const uint32_t* __restrict__ start, uint32_t cell_base,
+                                          uint32_t delta, int3 g, int r, uint32_t& jb, uint32_t& je) {
+    const int z = g.z + r / 3 - 1, y = g.y + r % 3 - 1;
+    if (z < 0 || z >= (int)P.gz || y < 0 || y >= (int)P.gy) return false;
+    const int x0 = max(g.x - 1, 0), x1 = min(g.x + 1, (int)P.gx - 1);
+    const uint32_t row = cell_base + (uint32_t)y * P.gx + (uint32_t)z * P.gxy;
+    jb = __ldg(start + row + x0) + delta;
+    je = __ldg(start + row + x1 + 1) + delta;
+    return true;
+}
+
+// Visit the candidates recorded in a particle's neighbour masks: one 32-bit
+// word per row, bit b = candidate jb+b lies within the skin radius
+// (1 + SPH_SKIN) h at the positions the masks were built from.  Rows longer
+// than 32 candidates carry no mask and are walked in full.  f(j) must apply
+// its own exact distance test.
+template <class F>
+__device__ __forceinline__ void for_masked(const DevParams& P, const uint32_t* __restrict__ start, uint32_t cell_base,
+                                           uint32_t delta, int3 g, const uint32_t* __restrict__ mask, size_t stride,
+                                           uint32_t k, F&& f) {
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        uint32_t jb, je;
+        if (!row_range(P, start, cell_base, delta, g, r, jb, je)) continue;
+        if (je - jb <= 32u) {
+            uint32_t bits = __ldg(mask + (size_t)r * stride + k);
+            while (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                f(jb + (uint32_t)b);
+            }
+        } else {
+            for (uint32_t j = jb; j < je; ++j) f(j);
+        }
+    }
+}
+
+// Tile scheduling of the scene-aware kernels.  With tile_ctr == nullptr each
+// block runs tile blockIdx.x; otherwise the launch is persistent (a few
+// blocks per SM) and blocks take tiles in turn from an atomic counter, which
+// balances scenes of uneven size.  body(tile) is called by every thread of
+// the block; a thread leaves a tile by returning from body.
+template <class Body>
+__device__ __forceinline__ void for_each_tile(const uint4* __restrict__ tiles, uint32_t ntiles,
+                                              uint32_t* __restrict__ tile_ctr, Body&& body) {
+    if (tile_ctr == nullptr) {
+        if (blockIdx.x < ntiles) body(tiles[blockIdx.x]);
+        return;
+    }
+    __shared__ uint32_t s_tile;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+        __syncthreads();
+        const uint32_t ti = s_tile;
+        __syncthreads();
+        if (ti >= ntiles) break;
+        body(tiles[ti]);
+    }
+}
+
 // Counter-based generator for lattice jitter: splitmix64 (Steele, Lea and
 // Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014).
 __host__ __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {

@@ -220,8 +220,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
                                                       const uint4* __restrict__ tiles,
                                                       const uint32_t* __restrict__ start,
                                                       const float4* __restrict__ P1, float4* __restrict__ S,
-                                                      uint32_t* __restrict__ nbr_out) {
-    const uint4 t = tiles[blockIdx.x];
+                                                      uint32_t* __restrict__ mask, size_t mask_stride,
+                                                      uint32_t* __restrict__ nbr_out, uint32_t ntiles,
+                                                      uint32_t* __restrict__ tile_ctr) {
+  for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
     const DevScene sc = scenes[t.x];
@@ -234,21 +236,39 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
         return;
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
-    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6;
+    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = pp.skin2;
     float sum = 0.0f;
     uint32_t cnt = 0;
-    for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
-        const float4 q = __ldg(P1 + j);
+    // Every candidate is tested here; the ones within the skin radius are
+    // recorded per row for the later passes (self excluded).
+    auto visit = [&](const float4& q, uint32_t j, uint32_t jb, uint32_t& bits) {
         const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
-        if (rr <= h2 && j != k) {
-            const float r = sqrtf(rr);
-            const float x = fmaf(-r, r, h2);
-            const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
-            sum = fmaf(mass, w, sum);
-            cnt++;
+        if (rr <= skin2 && j != k) {
+            if (j - jb < 32u) bits |= 1u << (j - jb);
+            if (rr <= h2) {
+                const float r = sqrtf(rr);
+                const float x = fmaf(-r, r, h2);
+                const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
+                sum = fmaf(mass, w, sum);
+                cnt++;
+            }
         }
-    });
+    };
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+        uint32_t jb, je, bits = 0u;
+        if (row_range(pp, start, sc.cell_base, delta, g, r, jb, je)) {
+            uint32_t j = jb;
+            for (; j + 2u <= je; j += 2u) {   // two independent loads in flight
+                const float4 q0 = __ldg(P1 + j), q1 = __ldg(P1 + j + 1u);
+                visit(q0, j, jb, bits);
+                visit(q1, j + 1u, jb, bits);
+            }
+            if (j < je) visit(__ldg(P1 + j), j, jb, bits);
+        }
+        mask[(size_t)r * mask_stride + k] = bits;
+    }
     const float d = fabsf(sdf_box(pp, p.x, p.y, p.z));
     float corr = sum;
     if (d < pp.h) corr = fmaf(pp.rest_density, 1.0f - boundary_density(pp, d), corr);
@@ -258,6 +278,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
     const float cs = pp.gas_constant * powf(ratio, pp.gamma - 1.0f);
     S[k] = make_float4(rho, prs, cs, 0.0f);
     if (nbr_out) nbr_out[k] = cnt;
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -270,8 +291,11 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
                                                       const uint4* __restrict__ tiles,
                                                       const uint32_t* __restrict__ start,
                                                       const float4* __restrict__ P1,
-                                                      const float4* __restrict__ S, float4* __restrict__ N) {
-    const uint4 t = tiles[blockIdx.x];
+                                                      const float4* __restrict__ S,
+                                                      const uint32_t* __restrict__ mask, size_t mask_stride,
+                                                      float4* __restrict__ N, uint32_t ntiles,
+                                                      uint32_t* __restrict__ tile_ctr) {
+  for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     const DevParams& pp = params[t.x];
     if (!(pp.flags & 1u)) return;
     if (threadIdx.x >= t.z) return;
@@ -285,7 +309,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+    for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, [&](uint32_t j) {
         const float4 q = __ldg(P1 + j);
         const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
@@ -302,6 +326,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
         }
     });
     N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -312,7 +337,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
 // force buffers in the reference's order, which after the swapped arguments
 // at fluidsystem.cu:352-364 is ((pressure + tension) + viscosity) + adhesion.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(SPH_TILE) k_force_integrate(const DevParams* __restrict__ params,
+// (256 threads, 3 blocks per SM: ptxas keeps it at 79 registers without spills;
+// with the default heuristic it caps at 64 and spills)
+__global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams* __restrict__ params,
                                                               const DevScene* __restrict__ scenes,
                                                               const uint4* __restrict__ tiles,
                                                               const uint32_t* __restrict__ start,
@@ -321,10 +348,14 @@ __global__ void __launch_bounds__(SPH_TILE) k_force_integrate(const DevParams* _
                                                               const float4* __restrict__ A1,
                                                               const float4* __restrict__ S,
                                                               const float4* __restrict__ N,
+                                                              const uint32_t* __restrict__ mask, size_t mask_stride,
                                                               float4* __restrict__ P0, float4* __restrict__ V2,
-                                                              float4* __restrict__ A0,
-                                                              float4* __restrict__ dbg_forces) {
-    const uint4 t = tiles[blockIdx.x];
+                                                              float4* __restrict__ A0, uint32_t* __restrict__ maxdisp,
+                                                              float4* __restrict__ dbg_forces, uint32_t ntiles,
+                                                              uint32_t* __restrict__ tile_ctr) {
+  for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
+    // lanes holding a particle of this tile (taken before any divergence)
+    const unsigned lanes = __ballot_sync(0xffffffffu, threadIdx.x < t.z);
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
     const DevScene sc = scenes[t.x];
@@ -344,7 +375,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_force_integrate(const DevParams* _
         float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
         if (tension) ni = N[k];
         const float h2 = pp.h2, eps = pp.eps;
-        for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+        for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, [&](uint32_t j) {
             const float4 pj = __ldg(P1 + j);
             const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
@@ -433,6 +464,34 @@ __global__ void __launch_bounds__(SPH_TILE) k_force_integrate(const DevParams* _
     P0[k] = make_float4(px, py, pz, si.x);
     V2[k] = make_float4(vx, vy, vz, 0.f);
     A0[k] = make_float4(anx, any, anz, 0.f);
+    // largest displacement of the substep in units of h (squared), for XSPH's
+    // use of the neighbour masks; NaN compares above every finite value
+    const float ddx = px - pi.x, ddy = py - pi.y, ddz = pz - pi.z;
+    const float d2 = dot3(ddx, ddy, ddz, ddx, ddy, ddz) * pp.inv_h2;
+    const uint32_t bits = (d2 != d2) ? 0x7fffffffu : __float_as_uint(d2);
+    const uint32_t wmax = __reduce_max_sync(lanes, bits);
+    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(lanes) - 1)) atomicMax(maxdisp, wmax);
+  });
+}
+
+// One XSPH pair term (fluidphysics.cu:392-401).
+__device__ __forceinline__ void xsph_pair(const float4* __restrict__ P0, const float4* __restrict__ V2, uint32_t j,
+                                          uint32_t k, const float4& pi, const float4& vi, float h2, float h, float c6,
+                                          float two_m, float eps, float& sx, float& sy, float& sz) {
+    const float4 q = __ldg(P0 + j);
+    const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+    const float rr = dot3(dx, dy, dz, dx, dy, dz);
+    const float rs = pi.w + q.w;
+    if (rr <= h2 && rs > eps && j != k) {
+        const float r = sqrtf(rr);
+        const float x = fmaf(-r, r, h2);
+        const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
+        const float coeff = w * (two_m / rs);
+        const float4 vj = __ldg(V2 + j);
+        sx = fmaf(coeff, vj.x - vi.x, sx);
+        sy = fmaf(coeff, vj.y - vi.y, sy);
+        sz = fmaf(coeff, vj.z - vi.z, sz);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -441,14 +500,18 @@ __global__ void __launch_bounds__(SPH_TILE) k_force_integrate(const DevParams* _
 // reference updates velocities in place while neighbours read them (a race);
 // here reads see V2 and the result goes to V0 (Jacobi).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(SPH_TILE) k_xsph(const DevParams* __restrict__ params,
+// (no __launch_bounds__: with it ptxas caps this kernel at 48 registers and spills)
+__global__ void k_xsph(const DevParams* __restrict__ params,
                                                    const DevScene* __restrict__ scenes,
                                                    const uint4* __restrict__ tiles,
                                                    const uint32_t* __restrict__ start,
                                                    const float4* __restrict__ P1,
                                                    const float4* __restrict__ P0,
-                                                   const float4* __restrict__ V2, float4* __restrict__ V0) {
-    const uint4 t = tiles[blockIdx.x];
+                                                   const float4* __restrict__ V2,
+                                                   const uint32_t* __restrict__ mask, size_t mask_stride,
+                                                   const uint32_t* __restrict__ maxdisp, float4* __restrict__ V0,
+                                                   uint32_t ntiles, uint32_t* __restrict__ tile_ctr) {
+  for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
     const DevScene sc = scenes[t.x];
@@ -464,23 +527,20 @@ __global__ void __launch_bounds__(SPH_TILE) k_xsph(const DevParams* __restrict__
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
     const float h2 = pp.h2, h = pp.h, c6 = pp.poly6, two_m = pp.two_mass, eps = pp.eps;
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
-        const float4 q = __ldg(P0 + j);
-        const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
-        const float rr = dot3(dx, dy, dz, dx, dy, dz);
-        const float rs = pi.w + q.w;
-        if (rr <= h2 && rs > eps && j != k) {
-            const float r = sqrtf(rr);
-            const float x = fmaf(-r, r, h2);
-            const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
-            const float coeff = w * (two_m / rs);
-            const float4 vj = __ldg(V2 + j);
-            sx = fmaf(coeff, vj.x - vi.x, sx);
-            sy = fmaf(coeff, vj.y - vi.y, sy);
-            sz = fmaf(coeff, vj.z - vi.z, sz);
-        }
-    });
+    // The masks hold every candidate within (1 + skin) h at the old
+    // positions; a pair can close to h after the move only if the particles
+    // moved less than skin*h/2 each, which the force pass recorded.
+    if (__uint_as_float(__ldg(maxdisp)) <= pp.xsph_disp_limit2) {
+        for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, [&](uint32_t j) {
+            xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
+        });
+    } else {
+        for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
+            xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
+        });
+    }
     V0[k] = make_float4(fmaf(pp.xsph, sx, vi.x), fmaf(pp.xsph, sy, vi.y), fmaf(pp.xsph, sz, vi.z), 0.f);
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -564,9 +624,10 @@ __global__ void k_sorted_keys(const uint32_t* __restrict__ key, const uint32_t* 
 // Launch wrappers.
 // ---------------------------------------------------------------------------
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st) {
-    k_hash<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.P0, a.count, a.key, a.slot, a.status);
+    k_hash<<<a.ntiles, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.P0, a.count, a.key, a.slot, a.status);
     return cudaGetLastError();
 }
+static inline uint32_t* ctr(const StepArgs& a, int k) { return a.tile_ctr ? a.tile_ctr + k : nullptr; }
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
     const uint32_t n = a.total_cells;
     const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
@@ -586,26 +647,30 @@ cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_s
     return cudaGetLastError();
 }
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
-    k_scatter<<<a.ntiles, SPH_TILE, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
-    k_rank_gather<<<a.ntiles, SPH_TILE, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.P1,
-                                                 a.V1, a.A1, a.perm, a.status);
+    k_scatter<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
+    k_rank_gather<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.P1,
+                                                a.V1, a.A1, a.perm, a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
-    k_density<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.dbg_nbr);
+    k_density<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask,
+                                              a.mask_stride, a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
 }
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
-    k_normals<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.N);
+    k_normals<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask,
+                                              a.mask_stride, a.N, a.ntiles, ctr(a, 1));
     return cudaGetLastError();
 }
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
-    k_force_integrate<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S,
-                                                     a.N, a.P0, a.V2, a.A0, a.dbg_forces);
+    k_force_integrate<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S,
+                                                      a.N, a.mask, a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp,
+                                                      a.dbg_forces, a.ntiles, ctr(a, 2));
     return cudaGetLastError();
 }
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st) {
-    k_xsph<<<a.ntiles, SPH_TILE, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.V0);
+    k_xsph<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.mask,
+                                           a.mask_stride, a.maxdisp, a.V0, a.ntiles, ctr(a, 3));
     return cudaGetLastError();
 }
 cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,

@@ -21,6 +21,12 @@ struct StepArgs {
     uint32_t *count, *start, *scan_sums;
     uint32_t *key, *slot, *tmp, *perm;
     uint32_t *status;
+    uint32_t *mask;            // 9 neighbour-mask words per slot, word r at mask[r*mask_stride + slot]
+    size_t mask_stride;
+    uint32_t *maxdisp;         // largest (displacement/h)^2 of the substep, float bits
+    uint32_t block;            // threads per block = particles per tile
+    uint32_t grid_nbr;         // blocks of the neighbour passes (ntiles, or the persistent grid)
+    uint32_t *tile_ctr;        // 4 tile counters for persistent neighbour passes, or nullptr
     uint32_t *dbg_nbr;         // optional: neighbour counts per sorted slot
     float4 *dbg_forces;        // optional: 4 force vectors per sorted slot
 };

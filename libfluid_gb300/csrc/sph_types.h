@@ -32,8 +32,17 @@ struct DevParams {
     float grav_x, grav_y, grav_z;
     float eps;                    // FLT_MIN (fluidparams.cu:48)
     uint32_t flags;               // bit0: surface tension active (normals pass needed)
+    float skin2;                  // ((1 + skin) h)^2: radius of the neighbour masks
+    float inv_h2;                 // 1/h^2, normalises displacements for the XSPH mask check
+    float xsph_disp_limit2;       // (skin/2)^2 * 0.98: largest (displacement/h)^2 XSPH may accept
     uint32_t pad_[3];
 };
+
+// Neighbour masks are built with radius (1 + skin) h (default skin below).
+// XSPH, which runs on positions moved by the integrator, may use them only
+// while every particle moved less than skin*h/2 in the substep (checked on
+// the device; otherwise XSPH walks all candidates).
+#define SPH_SKIN_DEFAULT 0.2f
 
 // Scene placement in the engine's arenas.
 struct DevScene {

@@ -17,8 +17,8 @@ LIB_PATH = os.path.join(_HERE, "liboracle.so")
 PARAMS = {"rest_density": 0, "particle_size": 1, "gas_constant": 2, "xsph": 3, "surface_tension": 4,
           "viscosity": 5, "adhesion": 6, "vdamp": 7, "gamma": 8, "mass": 9, "dt": 10}
 VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "normal": 3, "fpressure": 4, "ftension": 5, "fadhesion": 6,
-              "fviscosity": 7, "colour": 8}
-SCALAR_FIELDS = {"density": 16, "pressure": 17, "soundspeed": 18}
+              "fviscosity": 7, "colour": 8, "vel_int": 9}
+SCALAR_FIELDS = {"density": 16, "pressure": 17, "soundspeed": 18, "rho_sum": 19}
 U32_FIELDS = {"hash_pre": 32, "hash": 33, "perm": 34, "cellstart": 35, "cellocc": 36, "nbrcount": 37}
 STAGES = {"hash_sort": 0, "density": 1, "normals": 2, "forces": 3, "integrate": 4, "xsph": 5, "colour": 6}
 

@@ -277,8 +277,8 @@ struct SimBase {
 template <class T> struct Sim : SimBase {
     Params<T> P;
     bool isInit = false;
-    std::vector<V3<T>> pos, vel, acc, nrm, fp, ft, fa, fv, colour;
-    std::vector<T> rho, prs, cs;
+    std::vector<V3<T>> pos, vel, acc, nrm, fp, ft, fa, fv, colour, vint;   // vint: velocity before XSPH
+    std::vector<T> rho, prs, cs, rho_sum;   // rho_sum: neighbour sum before the boundary term
     std::vector<uint32_t> hash_pre, hash, perm, cellOcc, cellStart, nbr;
     uint64_t substeps_done = 0;
 
@@ -294,8 +294,8 @@ template <class T> struct Sim : SimBase {
         acc.assign(n, mk(T(0), T(0), T(0)));
         fp.assign(n, mk(T(0), T(0), T(0)));
         ft = fa = fv = fp;
-        colour = fp;
-        rho.assign(n, T(0)); prs.assign(n, T(0)); cs.assign(n, T(0));
+        colour = vint = fp;
+        rho.assign(n, T(0)); prs.assign(n, T(0)); cs.assign(n, T(0)); rho_sum.assign(n, T(0));
         hash_pre.assign(n, 0); hash.assign(n, 0); perm.resize(n);
         for (uint32_t i = 0; i < n; ++i) perm[i] = i;
         nbr.assign(n, 0);
@@ -388,6 +388,7 @@ template <class T> struct Sim : SimBase {
             const T d = std::fabs(sdf_box(P, pi));
             T corr = sum;
             if (d < P.h) corr = fma_(P.restDensity, T(1.0f) - boundary_density(P, d), corr);
+            rho_sum[i] = sum;
             rho[i] = (sum == T(0)) ? P.restDensity : corr;
             prs[i] = (corr == T(0)) ? T(0)
                    : (P.gasConstant * P.restDensity * P.invGamma) * (pow_(corr * P.invRestDensity, P.gamma) - T(1));
@@ -495,7 +496,7 @@ template <class T> struct Sim : SimBase {
                 const T k = (T(1.0f) + P.vdamp) * dot(nb, v);
                 v = fmaV(-k, nb, v);
             }
-            pos[i] = p; vel[i] = v; acc[i] = an;
+            pos[i] = p; vel[i] = v; acc[i] = an; vint[i] = v;
         }
     }
 
@@ -575,8 +576,8 @@ enum {
 };
 enum {
     ORC_F_POS = 0, ORC_F_VEL, ORC_F_ACC, ORC_F_NORMAL, ORC_F_FPRESSURE, ORC_F_FTENSION, ORC_F_FADHESION,
-    ORC_F_FVISCOSITY, ORC_F_COLOUR,                       // vec3 fields
-    ORC_F_DENSITY = 16, ORC_F_PRESSURE, ORC_F_SOUNDSPEED, // scalar fields
+    ORC_F_FVISCOSITY, ORC_F_COLOUR, ORC_F_VEL_INT,        // vec3 fields
+    ORC_F_DENSITY = 16, ORC_F_PRESSURE, ORC_F_SOUNDSPEED, ORC_F_RHOSUM, // scalar fields
     ORC_F_HASH_PRE = 32, ORC_F_HASH, ORC_F_PERM, ORC_F_CELLSTART, ORC_F_CELLOCC, ORC_F_NBRCOUNT  // u32
 };
 
@@ -714,9 +715,11 @@ int orc_get(void* s, int field, float* out_f32, double* out_f64, uint32_t* out_u
             case ORC_F_FADHESION: v3 = &S.fa; break;
             case ORC_F_FVISCOSITY: v3 = &S.fv; break;
             case ORC_F_COLOUR: v3 = &S.colour; break;
+            case ORC_F_VEL_INT: v3 = &S.vint; break;
             case ORC_F_DENSITY: sc = &S.rho; break;
             case ORC_F_PRESSURE: sc = &S.prs; break;
             case ORC_F_SOUNDSPEED: sc = &S.cs; break;
+            case ORC_F_RHOSUM: sc = &S.rho_sum; break;
             case ORC_F_HASH_PRE: u = &S.hash_pre; break;
             case ORC_F_HASH: u = &S.hash; break;
             case ORC_F_PERM: u = &S.perm; break;
