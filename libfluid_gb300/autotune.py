@@ -1,0 +1,101 @@
+"""Autotuner of the substep's launch configuration.
+
+Sweeps, on a GPU, the execution choices that do not change results (every
+choice computes bit-identical values; tests/test_exec_configs_gpu.py checks
+it): particles per tile (= threads per block), persistent blocks per SM for
+the neighbour passes (0 = one block per tile), and the neighbour-mask skin.
+Each candidate is timed with CUDA events over graph-replayed substeps after
+warm-up.  The best configuration per workload is written to tuned.json next
+to this file, which Batch and FluidSystem apply at creation.
+
+    python -m libfluid_gb300.autotune [--workload batched|dam_break_1m|all] [--steps 20]
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import os
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TUNED = os.path.join(HERE, "tuned.json")
+
+TILES = (128, 256)
+PERSISTENT = (0, 2, 4)
+SKINS = (0.1, 0.15, 0.2, 0.3)
+
+
+def load(workload: str) -> dict | None:
+    try:
+        return json.load(open(TUNED))[workload]["best"]
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def _scenes(workload: str):
+    from . import workloads as W
+    if workload == "batched":
+        return W.batch_manifest(num_scenes=256, seed=7)
+    if workload == "dam_break_1m":
+        return [W.dam_break_1m()]
+    if workload == "small_dam_break":
+        return [W.small_dam_break()]
+    raise ValueError(workload)
+
+
+def time_config(scenes, tile: int, persistent: int, skin: float, steps: int, warmup: int = 5,
+                device: int = 0) -> float:
+    from .batch import Batch
+    b = Batch(device)
+    b.set_exec(tile=tile, persistent=persistent, skin=skin)
+    for s in scenes:
+        b.add_scene(s)
+    for _ in range(warmup):
+        b.step(1)
+    b.sync()
+    b.timer_mark(0)
+    for _ in range(steps):
+        b.step_async(1)
+    b.timer_mark(1)
+    ms = b.timer_elapsed(0, 1) / steps
+    b.sync()
+    b.close()
+    return ms
+
+
+def tune(workload: str, steps: int = 20, device: int = 0) -> dict:
+    scenes = _scenes(workload)
+    n = sum(s.n for s in scenes)
+    trials = []
+    for tile, pers, skin in itertools.product(TILES, PERSISTENT, SKINS):
+        ms = time_config(scenes, tile, pers, skin, steps, device=device)
+        trials.append({"tile": tile, "persistent": pers, "skin": skin, "ms_per_step": ms,
+                       "particle_steps_per_s": n / (ms * 1e-3)})
+    best = min(trials, key=lambda t: t["ms_per_step"])
+    return {"workload": workload, "particles": n, "scenes": len(scenes), "steps": steps,
+            "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
+            "best": {k: best[k] for k in ("tile", "persistent", "skin")}, "trials": trials}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="all")
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--out", default=TUNED)
+    args = ap.parse_args()
+    names = ["dam_break_1m", "batched", "small_dam_break"] if args.workload == "all" else [args.workload]
+    try:
+        tuned = json.load(open(args.out))
+    except (OSError, ValueError):
+        tuned = {}
+    for w in names:
+        r = tune(w, args.steps)
+        tuned[w] = r
+        print(w, r["best"], "%.4f ms/step" % min(t["ms_per_step"] for t in r["trials"]), flush=True)
+    with open(args.out, "w") as f:
+        json.dump(tuned, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

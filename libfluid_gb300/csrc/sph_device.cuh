@@ -63,13 +63,16 @@ __device__ __forceinline__ float cohesion_k(const DevParams& P, float r) {
     if (sel != 0.0f) return hr3 * r * r * r;
     return 2.0f * hr3 * r * r * r - P.h6 * 0.0156f;
 }
-// boundaryDensity (fluidkernel.cu:45-67)
+// boundaryDensity (fluidkernel.cu:45-67), multiply-adds fused as the
+// reference build fuses them (see the oracle).
 __device__ __forceinline__ float boundary_density(const DevParams& P, float d) {
     if ((d > P.h) || (d < 0.0f)) return 0.0f;
     const float c = -d, c2 = c * c, c3 = c2 * c, c4 = c3 * c, c6 = c3 * c3;
-    const float poly = c3 * (35.0f * c6 - 180.0f * c4 * P.h2 + 378.0f * c2 * P.h4 - 420.0f * P.h6)
-                     + 315.0f * c * P.h8 + 128.0f * P.h9;
-    return 1.0f - 0.0039062f * P.invh9 * poly;
+    const float e1 = fmaf(35.0f, c6, -((180.0f * c4) * P.h2));
+    const float e2 = fmaf(378.0f * c2, P.h4, e1);
+    const float e3 = fmaf(-420.0f, P.h6, e2);
+    const float poly = fmaf(c3, e3, (315.0f * c) * P.h8) + 128.0f * P.h9;
+    return 1.0f - (0.0039062f * P.invh9) * poly;
 }
 
 // Grid coordinates of a position: floor(p * inv_cell) converted with

@@ -94,16 +94,24 @@ class SceneSpec:
     dt: float = 2e-4
     steps: int = 200
     unit_cube_res: int = 0          # >0: the reference's unit cube with res cells instead of box/h
+    extra_pos: np.ndarray | None = None   # host-generated particles after the blocks (e.g. spheres)
+    extra_vel: np.ndarray | None = None
 
     @property
     def n(self) -> int:
-        return sum(b.n for b in self.blocks)
+        return sum(b.n for b in self.blocks) + (0 if self.extra_pos is None else int(self.extra_pos.shape[0]))
 
     def positions(self) -> np.ndarray:
-        return np.concatenate([b.positions() for b in self.blocks])
+        parts = [b.positions() for b in self.blocks]
+        if self.extra_pos is not None:
+            parts.append(np.asarray(self.extra_pos, np.float32))
+        return np.concatenate(parts)
 
     def velocities(self) -> np.ndarray:
-        return np.concatenate([b.velocities() for b in self.blocks])
+        parts = [b.velocities() for b in self.blocks]
+        if self.extra_pos is not None:
+            parts.append(np.asarray(self.extra_vel, np.float32))
+        return np.concatenate(parts)
 
     def params(self) -> dict:
         return dict(rest_density=self.rest_density, mass=self.mass, gamma=self.gamma,
@@ -141,8 +149,17 @@ def large_tension(seed: int = 1) -> SceneSpec:
     0.9 m, z up) plus two spheres of radius 0.229 m falling at 1 m/s, spacing
     0.005 m, h = 0.01 m, box 1x1x2 m, c0 = 25 m/s, dt = 8e-5 s."""
     pool = Lattice(lo=(0.0, 0.0, 0.0), spacing=0.005, nx=200, ny=200, nz=180, jitter=0.05 * 0.005, seed=seed)
+    spheres = [sphere_sites(c, 0.229, 0.005) for c in ((0.27, 0.5, 1.3), (0.73, 0.5, 1.6))]
+    sp = np.concatenate(spheres)
+    rng_seed = np.uint64(seed) * np.uint64(2654435761)
+    ctr = np.arange(3 * sp.shape[0], dtype=np.uint64).reshape(-1, 3)
+    jit = ((np.float32(2.0) * uniform01(int(rng_seed), ctr) - np.float32(1.0)) *
+           np.float32(0.05 * 0.005)).astype(np.float32)
+    sp = (sp + jit).astype(np.float32)
+    sv = np.tile(np.asarray((0.0, 0.0, -1.0), np.float32), (sp.shape[0], 1))
     return SceneSpec(box=(1.0, 1.0, 2.0), h=0.01, blocks=[pool], mass=1.25e-4, particle_size=0.0025,
-                     gas_constant=625.0, surface_tension=0.0728, gravity=(0.0, 0.0, -9.81), dt=8e-5, steps=500)
+                     gas_constant=625.0, surface_tension=0.0728, gravity=(0.0, 0.0, -9.81), dt=8e-5, steps=500,
+                     extra_pos=sp, extra_vel=sv)
 
 
 def sphere_sites(center, radius, spacing):

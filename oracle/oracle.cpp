@@ -227,13 +227,19 @@ template <class T> inline T cohesion_k(const Params<T>& P, T r) {
     return T(2) * hr3 * r * r * r - P.h6 * T(0.0156f);
 }
 // fluidkernel.cu:45-67.  The leading 1.0 is a double literal: for the float
-// build the difference is formed in double and rounded once to float.
+// build the difference is formed in double and rounded once to float.  The
+// polynomial is evaluated with the multiply-adds fused the way the reference
+// build fuses them (matched against its outputs in tests/golden/):
+//   e1 = fma(35, c6, -(180 c4) h2); e2 = fma(378 c2, h4, e1);
+//   e3 = fma(-420, h6, e2); f = fma(c3, e3, (315 c) h8) + 128 h9.
 template <class T> inline T boundary_density(const Params<T>& P, T d) {
     if ((d > P.h) || (d < T(0))) return T(0);
     const T c = -d, c2 = c * c, c3 = c2 * c, c4 = c3 * c, c6 = c3 * c3;
-    const T poly = c3 * (T(35) * c6 - T(180) * c4 * P.h2 + T(378) * c2 * P.h4 - T(420) * P.h6)
-                 + T(315) * c * P.h8 + T(128) * P.h9;
-    const T f = T(0.0039062f) * P.invh9 * poly;
+    const T e1 = fma_(T(35), c6, -((T(180) * c4) * P.h2));
+    const T e2 = fma_(T(378) * c2, P.h4, e1);
+    const T e3 = fma_(T(-420), P.h6, e2);
+    const T poly = fma_(c3, e3, (T(315) * c) * P.h8) + T(128) * P.h9;
+    const T f = (T(0.0039062f) * P.invh9) * poly;
     return T(1.0 - double(f));
 }
 
