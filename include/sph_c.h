@@ -132,6 +132,8 @@ int sph_set_params(sph_system* s, const sph_params* p);
  * surface_tension, viscosity, adhesion, vdamp, vel_limit, acc_limit,
  * gravity xyz, eps.  Returns the number written. */
 int sph_get_derived(const sph_system* s, double* out, int cap);
+/* The same derivation for a parameter set, without a device (host only). */
+int sph_derive_params(const sph_params* p, double* out, int cap);
 
 /* ---- parity / debug taps ----------------------------------------------- */
 /* Per-particle and per-cell intermediates of the last substep, indexed like

@@ -321,10 +321,31 @@ int sph_set_params(sph_system* s, const sph_params* o) {
     return push_cfg(s);
 }
 
+static int derived_values(const SceneConfig& cfg, double* out, int cap);
+
 int sph_get_derived(const sph_system* s, double* out, int cap) {
     if (!s || !out) return 0;
+    return derived_values(s->cfg, out, cap);
+}
+
+int sph_derive_params(const sph_params* o, double* out, int cap) {
+    if (!o || !out) return 0;
+    SceneConfig c;
+    c.box_mode = (int)o->box_mode;
+    c.res = o->res;
+    c.lx = o->lx; c.ly = o->ly; c.lz = o->lz; c.h = o->h;
+    c.rest_density = o->rest_density; c.gas_constant = o->gas_constant; c.gamma = o->gamma;
+    c.mass = o->mass; c.particle_size = o->particle_size;
+    c.xsph = o->xsph; c.surface_tension = o->surface_tension; c.viscosity = o->viscosity;
+    c.adhesion = o->adhesion; c.vdamp = o->vdamp;
+    c.vel_limit = o->vel_limit; c.acc_limit = o->acc_limit; c.dt = o->dt;
+    c.gravity[0] = o->gravity[0]; c.gravity[1] = o->gravity[1]; c.gravity[2] = o->gravity[2];
+    return derived_values(c, out, cap);
+}
+
+static int derived_values(const SceneConfig& cfg, double* out, int cap) {
     DevParams p;
-    if (!sph::derive_params(s->cfg, p, nullptr)) return 0;
+    if (!sph::derive_params(cfg, p, nullptr)) return 0;
     const double v[] = {double(p.gx), double(p.gy), double(p.gz), double(p.inv_cell), double(p.h), double(p.h2),
                         double(p.poly6), double(p.grad_poly6), double(p.grad_spiky), double(p.cohesion),
                         double(p.invh9), double(p.rest_density), double(p.gas_constant), double(p.gamma),

@@ -106,8 +106,18 @@ void sph_server::loop() {
             }
         }
         // create admitted scenes (engine calls only on this thread)
-        for (Request* r : admit) {
+        for (size_t ai = 0; ai < admit.size(); ++ai) {
+            Request* r = admit[ai];
             int rc = eng->add_scene(r->cfg, r->n, &r->scene);
+            if (rc == sph::ENG_ENOMEM && !live.empty()) {
+                // the arena is fragmented or full: wait for running scenes to leave
+                std::lock_guard<std::mutex> lk(mu);
+                for (size_t b = admit.size(); b-- > ai;) {
+                    used_bytes -= admit[b]->bytes;
+                    queue.push_front(admit[b]);
+                }
+                break;
+            }
             if (rc == sph::ENG_OK) {
                 if (!r->pos.empty()) {
                     rc = eng->set_state(r->scene, r->pos.data(), r->vel.empty() ? nullptr : r->vel.data(), r->n);

@@ -155,6 +155,68 @@ __device__ __forceinline__ void for_masked(const DevParams& P, const uint32_t* _
     }
 }
 
+// Candidate walk over one of a particle's mask sets, flattened across the 9
+// rows: next() yields the next recorded candidate, moving to the next row
+// inside the same call, so lanes of a warp never wait for each other at row
+// boundaries.  Rows longer than 32 candidates carry no mask and yield every
+// candidate (the caller's exact test decides).
+struct MaskWalk {
+    const DevParams& P;
+    const uint32_t* __restrict__ start;
+    uint32_t cell_base, delta;
+    int3 g;
+    const uint32_t* __restrict__ mask;
+    size_t stride;
+    uint32_t k;
+    int r;
+    uint32_t jb, je, j, bits;
+    bool full;
+    __device__ __forceinline__ MaskWalk(const DevParams& P_, const uint32_t* __restrict__ start_, uint32_t cb,
+                                        uint32_t delta_, int3 g_, const uint32_t* __restrict__ mask_, size_t stride_,
+                                        uint32_t k_)
+        : P(P_), start(start_), cell_base(cb), delta(delta_), g(g_), mask(mask_), stride(stride_), k(k_), r(-1),
+          jb(0), je(0), j(0), bits(0), full(false) {}
+    __device__ __forceinline__ bool next(uint32_t& cand) {
+        for (;;) {
+            if (full) {
+                if (j < je) { cand = j++; return true; }
+                full = false;
+            } else if (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                cand = jb + (uint32_t)b;
+                return true;
+            }
+            if (++r >= 9) return false;
+            if (!row_range(P, start, cell_base, delta, g, r, jb, je)) continue;
+            if (je - jb <= 32u) bits = __ldg(mask + (size_t)r * stride + k);
+            else { full = true; j = jb; }
+        }
+    }
+};
+
+// Walk of every candidate of the 27 cells, flattened across the 9 rows.
+struct RangeWalk {
+    const DevParams& P;
+    const uint32_t* __restrict__ start;
+    uint32_t cell_base, delta;
+    int3 g;
+    int r;
+    uint32_t j, je;
+    __device__ __forceinline__ RangeWalk(const DevParams& P_, const uint32_t* __restrict__ start_, uint32_t cb,
+                                         uint32_t delta_, int3 g_)
+        : P(P_), start(start_), cell_base(cb), delta(delta_), g(g_), r(-1), j(0), je(0) {}
+    __device__ __forceinline__ bool next(uint32_t& cand) {
+        for (;;) {
+            if (j < je) { cand = j++; return true; }
+            if (++r >= 9) return false;
+            uint32_t jb;
+            if (!row_range(P, start, cell_base, delta, g, r, jb, je)) { j = je = 0; continue; }
+            j = jb;
+        }
+    }
+};
+
 // Tile scheduling of the scene-aware kernels.  With tile_ctr == nullptr each
 // block runs tile blockIdx.x; otherwise the launch is persistent (a few
 // blocks per SM) and blocks take tiles in turn from an atomic counter, which

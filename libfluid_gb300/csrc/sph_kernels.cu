@@ -236,38 +236,47 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
         return;
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
-    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = pp.skin2;
+    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = pp.skin2, eps = pp.eps;
     float sum = 0.0f;
     uint32_t cnt = 0;
-    // Every candidate is tested here; the ones within the skin radius are
-    // recorded per row for the later passes (self excluded).
-    auto visit = [&](const float4& q, uint32_t j, uint32_t jb, uint32_t& bits) {
+    // Every candidate is tested here and recorded per row for the later
+    // passes: mask words 0-8 hold the candidates within the skin radius
+    // (XSPH), words 9-17 the exact neighbours j != i, eps < r^2 <= h^2 (the
+    // normal and force passes' test, evaluated bit for bit the same way).
+    // One loop runs across all 9 rows so lanes do not wait at row ends.
+    int r = -1;
+    uint32_t jb = 0, j = 0, je = 0, bs = 0u, be = 0u;
+    bool valid = false;
+    for (;;) {
+        if (j >= je) {
+            if (valid) {
+                mask[(size_t)r * mask_stride + k] = bs;
+                mask[(size_t)(9 + r) * mask_stride + k] = be;
+            }
+            if (++r >= 9) break;
+            bs = be = 0u;
+            valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
+            if (!valid) jb = je = 0;
+            j = jb;
+            continue;
+        }
+        const float4 q = __ldg(P1 + j);
         const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
         if (rr <= skin2 && j != k) {
-            if (j - jb < 32u) bits |= 1u << (j - jb);
+            const uint32_t off = j - jb;
+            const uint32_t bit = (off < 32u) ? (1u << off) : 0u;
+            bs |= bit;
             if (rr <= h2) {
-                const float r = sqrtf(rr);
-                const float x = fmaf(-r, r, h2);
-                const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
+                if (rr > eps) be |= bit;
+                const float rd = sqrtf(rr);
+                const float x = fmaf(-rd, rd, h2);
+                const float w = (rd >= h) ? 0.0f : c6 * (x * x * x);
                 sum = fmaf(mass, w, sum);
                 cnt++;
             }
         }
-    };
-#pragma unroll 1
-    for (int r = 0; r < 9; ++r) {
-        uint32_t jb, je, bits = 0u;
-        if (row_range(pp, start, sc.cell_base, delta, g, r, jb, je)) {
-            uint32_t j = jb;
-            for (; j + 2u <= je; j += 2u) {   // two independent loads in flight
-                const float4 q0 = __ldg(P1 + j), q1 = __ldg(P1 + j + 1u);
-                visit(q0, j, jb, bits);
-                visit(q1, j + 1u, jb, bits);
-            }
-            if (j < je) visit(__ldg(P1 + j), j, jb, bits);
-        }
-        mask[(size_t)r * mask_stride + k] = bits;
+        ++j;
     }
     const float d = fabsf(sdf_box(pp, p.x, p.y, p.z));
     float corr = sum;
@@ -276,7 +285,8 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
     const float ratio = corr * pp.inv_rest_density;
     const float prs = (corr == 0.0f) ? 0.0f : pp.eos_k * (powf(ratio, pp.gamma) - 1.0f);
     const float cs = pp.gas_constant * powf(ratio, pp.gamma - 1.0f);
-    S[k] = make_float4(rho, prs, cs, 0.0f);
+    // w = 1/rho^2, used by the force pass for p_j/rho_i^2 + p_i/rho_j^2
+    S[k] = make_float4(rho, prs, cs, 1.0f / (rho * rho));
     if (nbr_out) nbr_out[k] = cnt;
   });
 }
@@ -309,7 +319,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, [&](uint32_t j) {
+    MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
+    uint32_t j;
+    while (walk.next(j)) {
         const float4 q = __ldg(P1 + j);
         const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
@@ -324,7 +336,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
                 sz = sz + (s * rz) / den;
             }
         }
-    });
+    }
     N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
   });
 }
@@ -374,8 +386,11 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
         const float ri = si.x, pri = si.y, csi = si.z;
         float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
         if (tension) ni = N[k];
-        const float h2 = pp.h2, eps = pp.eps;
-        for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, [&](uint32_t j) {
+        const float h2 = pp.h2, eps = pp.eps, inv_ri2 = si.w;
+        // exact neighbours recorded by the density pass (mask words 9-17)
+        MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
+        uint32_t j;
+        while (walk.next(j)) {
             const float4 pj = __ldg(P1 + j);
             const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
@@ -386,12 +401,13 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
                     const float r = sqrtf(r2);
                     const float inv_r = 1.0f / r;
                     const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
-                    float Pi = 0.0f;
-                    if (ux < 0.0f) {
-                        const float mu = (pp.h * ux) / (r2 + pp.visc_eps);
-                        Pi = (-pp.viscosity * (csi + sj.z) * mu) / (ri + sj.x);
-                    }
-                    const float mid = sj.y / (ri * ri) + pri / (sj.x * sj.x);
+                    // artificial viscosity, only for approaching pairs; evaluated
+                    // without a branch (finite for every pair) and selected
+                    const float mu = (pp.h * ux) / (r2 + pp.visc_eps);
+                    const float Pv = (-pp.viscosity * (csi + sj.z) * mu) / (ri + sj.x);
+                    const float Pi = (ux < 0.0f) ? Pv : 0.0f;
+                    // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
+                    const float mid = sj.y * inv_ri2 + pri * sj.w;
                     const float s = pp.mass * grad_spiky(pp, r);
                     const float cx = (s * rx) * inv_r, cy = (s * ry) * inv_r, cz = (s * rz) * inv_r;
                     fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
@@ -414,7 +430,7 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
                     }
                 }
             }
-        });
+        }
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
         ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
         const float z = -fminf(sdf_box(pp, pi.x, pi.y, pi.z), 0.0f) * 0.25f * pp.inv_particle_size;
@@ -530,14 +546,13 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
     // The masks hold every candidate within (1 + skin) h at the old
     // positions; a pair can close to h after the move only if the particles
     // moved less than skin*h/2 each, which the force pass recorded.
+    uint32_t j;
     if (__uint_as_float(__ldg(maxdisp)) <= pp.xsph_disp_limit2) {
-        for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, [&](uint32_t j) {
-            xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
-        });
+        MaskWalk walk(pp, start, sc.cell_base, delta, g, mask, mask_stride, k);   // skin mask, words 0-8
+        while (walk.next(j)) xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
     } else {
-        for_candidates(pp, start, sc.cell_base, delta, g, [&](uint32_t j) {
-            xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
-        });
+        RangeWalk walk(pp, start, sc.cell_base, delta, g);
+        while (walk.next(j)) xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
     }
     V0[k] = make_float4(fmaf(pp.xsph, sx, vi.x), fmaf(pp.xsph, sy, vi.y), fmaf(pp.xsph, sz, vi.z), 0.f);
   });

@@ -21,7 +21,8 @@ struct StepArgs {
     uint32_t *count, *start, *scan_sums;
     uint32_t *key, *slot, *tmp, *perm;
     uint32_t *status;
-    uint32_t *mask;            // 9 neighbour-mask words per slot, word r at mask[r*mask_stride + slot]
+    uint32_t *mask;            // 18 neighbour-mask words per slot, word r at mask[r*mask_stride + slot]:
+                               // 0-8 skin radius (XSPH), 9-17 exact neighbours (normals, forces)
     size_t mask_stride;
     uint32_t *maxdisp;         // largest (displacement/h)^2 of the substep, float bits
     uint32_t block;            // threads per block = particles per tile

@@ -42,7 +42,7 @@ struct DevParams {
 // XSPH, which runs on positions moved by the integrator, may use them only
 // while every particle moved less than skin*h/2 in the substep (checked on
 // the device; otherwise XSPH walks all candidates).
-#define SPH_SKIN_DEFAULT 0.2f
+#define SPH_SKIN_DEFAULT 0.1f
 
 // Scene placement in the engine's arenas.
 struct DevScene {

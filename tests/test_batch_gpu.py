@@ -22,7 +22,8 @@ def _mix(count=6, seed=3):
     specs[1].box = (1.0, 1.0, 1.0)
     specs[2].surface_tension = 0.0
     specs[3].surface_tension = 0.05
-    specs[4].adhesion = 0.2
+    if count > 4:
+        specs[4].adhesion = 0.2
     return specs
 
 

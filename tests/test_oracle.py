@@ -1,0 +1,190 @@
+"""CPU known-answer tests of the oracle and of the library's host logic,
+restated from the reference sources (cited per test).  No GPU needed."""
+import ctypes as C
+import hashlib
+
+import numpy as np
+import pytest
+
+import oracle
+from libfluid_gb300 import _capi, workloads as W
+from libfluid_gb300.batch import params_struct
+
+f32 = np.float32
+
+
+def _orc(n=1, res=10):
+    o = oracle.Oracle(32)
+    o.init(n, res)
+    return o
+
+
+def test_init_defaults_fluidsystem_init():
+    # fluidsystem.cu:210-235 reset values; FluidParams ctor leaves tension 1,
+    # viscosity 0.1, adhesion 1 (fluidparams.cuh:88-90)
+    p = _orc(8, 16).params()
+    gx, gy, gz, inv_cell, h = p[0], p[1], p[2], p[3], p[4]
+    assert (gx, gy, gz) == (16, 16, 16) and inv_cell == 16.0
+    assert h == float(f32(1.0) / f32(16.0))
+    rest, gas, gamma, mass, psize, dt, xsph, tension, visc, adh, vdamp, vlim, alim = p[11:24]
+    assert (rest, gas, gamma, mass, psize, dt, xsph) == (1000.0, 100.0, 7.0, 1.0, 1.0, 1.0, 0.5)
+    assert (float(f32(tension)), float(f32(visc)), float(f32(adh)), vdamp) == (1.0, float(f32(0.1)), 1.0, 0.0)
+    assert (vlim, alim) == (5.0, 150.0)
+    assert tuple(p[24:27]) == (0.0, float(f32(-9.8)), 0.0)
+    assert p[27] == float(np.finfo(np.float32).tiny)
+
+
+def test_kernel_coefficients_fluidparams_setres():
+    # fluidparams.cu:80-86 evaluated in float with the host C library's powf
+    libm = C.CDLL("libm.so.6")
+    libm.powf.restype = C.c_float
+    libm.powf.argtypes = [C.c_float, C.c_float]
+    p = _orc(1, 50).params()
+    h = f32(1.0) / f32(50.0)
+    pi = f32(3.141592654)
+    assert p[6] == float(f32(315.0) / (f32(64.0) * pi * f32(libm.powf(float(h), 9.0))))
+    assert p[8] == float(f32(-45.0) / (pi * f32(libm.powf(float(h), 6.0))))
+
+
+def test_library_and_oracle_derive_identical_parameters():
+    for spec in (W.small_dam_break(), W.small_dam_break(unit_cube=True), W.dam_break_1m(), W.large_tension()):
+        sp = params_struct(spec)
+        buf = (C.c_double * 64)()
+        k = _capi.lib().sph_derive_params(C.byref(sp), buf, 64)
+        lib_vals = np.array(buf[:k])
+        o = oracle.Oracle(32)
+        o.init(1, spec.unit_cube_res or 1)
+        if not spec.unit_cube_res:
+            o.set_domain(*spec.box, spec.h)
+        for key, v in spec.params().items():
+            if key == "gravity":
+                o.set_gravity(*v)
+            elif key not in ("vel_limit", "acc_limit"):
+                o.set_param(key, v)
+        o.set_limits(spec.vel_limit, spec.acc_limit)
+        assert np.array_equal(lib_vals, o.params()), spec
+
+
+def test_substep_count_oracle_equals_library():
+    L = _capi.lib()
+    for full, sub in [(0.01, 10), (2e-4, 1), (0.002, 3), (0.1, 7), (1.0, 1000)]:
+        assert oracle.substep_count(full, sub) == L.sph_substep_count(C.c_float(full), sub)
+
+
+def _one_step(pos, vel=None, res=10, **params):
+    n = len(pos)
+    o = _orc(n, res)
+    for k, v in params.items():
+        o.set_param(k, v)
+    o.set_state(np.asarray(pos, np.float32), None if vel is None else np.asarray(vel, np.float32))
+    o.advance(1e-4, 1)
+    return o
+
+
+def test_hash_cells_nulls_and_faces():
+    # grid = floor(p*res), x fastest; outside [0,1)^3 -> NULL_HASH (hash.cu:10-27)
+    pts = [(0.0, 0.0, 0.0), (0.1, 0.2, 0.3), (0.999, 0.5, 0.05), (1.0, 0.5, 0.5), (-1e-3, 0.5, 0.5),
+           (0.5, 0.5, 2.0), (0.35, 0.35, 0.35)]
+    o = _orc(len(pts), 10)
+    o.set_state(np.array(pts, np.float32))
+    o.stage("hash_sort")
+    hp = o.get("hash_pre")
+    assert hp[0] == 0
+    assert hp[1] == 1 + 2 * 10 + 3 * 100      # 0.1*10 = 1 exactly on the face
+    assert hp[2] == 9 + 5 * 10 + 0 * 100
+    assert list(hp[3:6]) == [0xFFFFFFFF] * 3
+    assert hp[6] == 3 + 3 * 10 + 3 * 100
+
+
+def test_sort_is_stable_and_nulls_last():
+    # thrust::sort_by_key on u32 keys keeps equal keys in order (fluidsystem.cu:309-313)
+    pts = np.array([(0.55, 0.55, 0.55), (0.05, 0.05, 0.05), (2.0, 0, 0), (0.56, 0.51, 0.52),
+                    (0.06, 0.02, 0.07), (0.57, 0.53, 0.59), (-1, 0, 0)], np.float32)
+    o = _orc(len(pts), 10)
+    o.set_state(pts)
+    o.stage("hash_sort")
+    assert list(o.get("perm")) == [1, 4, 0, 3, 5, 2, 6]
+    h = o.get("hash")
+    assert list(h[:5]) == [0, 0, 555, 555, 555] and list(h[5:]) == [0xFFFFFFFF] * 2
+    occ, start = o.get("cellocc"), o.get("cellstart")
+    assert occ[0] == 2 and occ[555] == 3 and occ.sum() == 5
+    assert start[555] == 2 and start[556] == 5
+
+
+def test_boundary_density_limits():
+    # fluidkernel.cu:45-67: 0.5 at the wall, ~1 at one smoothing length
+    o = _orc(1, 10)
+    # a single particle far from other particles: density = rho0*(1 - bd(d)) when d < h
+    for y, expect in ((0.0, 0.5 * 1000.0), (0.1 + 1e-6, 0.0)):
+        o.set_state(np.array([(0.5, y, 0.5)], np.float32))
+        o.stage("hash_sort")
+        o.stage("density")
+        rho = o.get("density")[0]
+        # sum == 0 -> density reported as rho0 (fluidphysics.cu:63)
+        assert rho == 1000.0
+    # the pressure uses the corrected density: p(d=0) = K*(0.5^7 - 1)
+    o.set_state(np.array([(0.5, 0.0, 0.5)], np.float32))
+    o.stage("hash_sort")
+    o.stage("density")
+    k = 100.0 * 1000.0 / 7.0
+    assert abs(o.get("pressure")[0] - k * (0.5 ** 7 - 1.0)) < 1e-3 * k
+
+
+def test_cohesion_precedence_quirk():
+    # fluidkernel.cu:37: coefficient * (r > h/2) only selects the branch, so for
+    # r <= h/2 the kernel is 2(h-r)^3 r^3 - 0.0156 h^6 (and negative for small r)
+    h = 0.1
+    pts = np.array([(0.5, 0.5, 0.5), (0.5 + 0.02, 0.5, 0.5)], np.float32)
+    o = _one_step(pts, res=10, surface_tension=1.0, mass=0.02, viscosity=0.0, adhesion=0.0, xsph=0.0,
+                  particle_size=0.001)
+    ft = o.get("ftension")
+    r = 0.02
+    coh = 2 * (h - r) ** 3 * r ** 3 - h ** 6 * 0.0156
+    assert coh < 0 and ft[0, 0] != 0.0
+
+
+def test_create_fluid_block_mass_and_size():
+    # fluidsystem.cu:84-108: mass = volume/n * rho0, particle size = diameter/2
+    o = _orc(1000, 16)
+    o.create_block(0, 1000, 0.1, 0.1, 0.1, 0.5, 0.5, 0.5)
+    p = o.params()
+    vol = f32(f32(f32(0.4) * f32(0.4)) * f32(0.4))
+    assert p[14] == float(f32(vol / f32(1000.0)) * f32(1000.0))
+    pos = o.get("pos")
+    assert np.all(pos >= 0.1) and np.all(pos <= 0.5)
+    assert 0.0 < p[15] < 0.05
+
+
+def test_fp32_oracle_within_tolerance_of_fp64():
+    spec = W.small_dam_break()
+    from helpers import configure_oracle
+    o32 = configure_oracle(oracle.Oracle(32), spec)
+    o64 = configure_oracle(oracle.Oracle(64), spec)
+    o32.advance(spec.dt, 1)
+    o64.advance(spec.dt, 1)
+    for f in ("hash", "perm", "nbrcount"):
+        assert np.array_equal(o32.get(f), o64.get(f))
+    r32, r64 = o32.get("density"), o64.get("density")
+    assert np.max(np.abs(r32 - r64) / r64) < 1e-5
+
+
+def test_lattice_generator_is_stable():
+    # the seeded generator defines every workload; its output must never drift
+    p = W.small_dam_break().positions()
+    assert p.shape == (32768, 3) and p.dtype == np.float32
+    digest = hashlib.sha256(p.tobytes()).hexdigest()
+    assert digest == _LATTICE_SHA256, digest
+
+
+def test_batch_manifest_shapes():
+    specs = W.batch_manifest(256, seed=7)
+    ns = np.array([s.n for s in specs])
+    assert len(specs) == 256 and ns.min() >= 1000 and ns.max() <= 80000
+    assert 3.5e6 < ns.sum() < 6.5e6
+    for s in specs:
+        (b,) = s.blocks
+        assert s.box[0] == pytest.approx(2 * b.nx * b.spacing) and s.box[1] == pytest.approx(1.2 * b.ny * b.spacing)
+        assert 0.005 <= s.viscosity <= 0.05 and 0.0 <= s.surface_tension <= 0.07
+
+
+_LATTICE_SHA256 = "b48b96bbb22a8c30a10ad69c042322382acbb27e722672b682def8a1479bce9c"

@@ -48,9 +48,16 @@ def test_results_identical_alone_and_in_the_mix():
     srv.close()
 
 
+def _request_bytes(s):
+    # the server's footprint of a scene: particle slots, cells + NULL bucket, tile entries
+    cells = int(np.prod([int(np.ceil(b / s.h - 1e-3)) for b in s.box]))
+    return s.n * 196 + (cells + 1) * 8 + (s.n // 64 + 1) * 16
+
+
 def test_admission_respects_memory_budget():
     specs = W.batch_manifest(num_scenes=5, seed=9, nmin=4000, nmax=4100, steps=6)
-    per_scene = max(s.n for s in specs) * 196 + 40000 * 8
+    per_scene = max(_request_bytes(s) for s in specs)
+    # room for two scenes, never three
     srv = Server(0, memory_budget=int(2.5 * per_scene))
     ids = [srv.submit(s, 6) for s in specs]
     assert srv.drain(60000)
