@@ -188,6 +188,9 @@ def workload(name: str):
         return W.dam_break_1m(unit_cube=True), "1M dam break in the reference's unit cube (res 100, h=0.01 m)"
     if name == "small_dam_break":
         return W.small_dam_break(), "32,768-particle dam break in a 1.0x0.6x0.6 m box, h=0.02 m, dt=2e-4 s"
+    if name == "large_tension":
+        return W.large_tension(), ("8,005,232 particles with surface tension 0.0728: 200x200x180 lattice pool plus "
+                                   "falling spheres, h=0.01 m, dt=8e-5 s")
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -390,8 +393,11 @@ def run_batched(args, dist):
     launch per pass, against the plain step run one scene at a time."""
     from libfluid_gb300 import workloads as W
     from libfluid_gb300.batch import Batch
+    from libfluid_gb300 import autotune
     specs = W.batch_manifest(num_scenes=args.scenes, seed=7)
+    exe = autotune.load("batched") or {}
     b = Batch(dist.local)
+    b.set_exec(**exe)
     for s in specs:
         b.add_scene(s)
     total_n = sum(s.n for s in specs)
@@ -414,6 +420,7 @@ def run_batched(args, dist):
     plain_ms = 0.0
     for s in specs:
         one = Batch(dist.local)
+        one.set_exec(**exe)
         one.add_scene(s)
         for _ in range(3):
             one.step(1)
@@ -431,7 +438,8 @@ def run_batched(args, dist):
             "config": {"workload": f"{len(specs)} dam-break scenes, particles log-uniform [2048, 65536], aspect "
                                    "[0.5,2], box 2x/1.2x the block, visc U[0.005,0.05], tension U[0,0.07], "
                                    "spacing 0.01 m, h 0.02 m, dt 2e-4 s", "scenes": len(specs),
-                       "particles": total_n, "timing": "CUDA events, graph replay, one launch per pass"},
+                       "particles": total_n, "timing": "CUDA events, graph replay, one launch per pass",
+                       "exec": exe or "engine defaults"},
             "plain_one_at_a_time": {"value": plain, "steps": k_plain,
                                     "how": "each scene alone in its own engine, graph replay, summed device time"},
             "speedup_vs_plain": value / plain, "clocks": clk}

@@ -165,12 +165,17 @@ int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
  * the same values bit for bit).  tile: particles per tile = threads per
  * block (64, 128 or 256); persistent: 0 = one block per tile, k > 0 = k
  * blocks per SM taking tiles from a counter in the neighbour passes; skin:
- * neighbour-mask skin in units of h, in (0, 1]. */
+ * neighbour-mask skin in units of h, in (0, 1]; variant: SPH_VARIANT_* bits
+ * choosing how the neighbour walks are scheduled.  Defaults: tile 128,
+ * persistent 0, skin 0.1, variant 3 (per-row density and XSPH walks). */
+#define SPH_VARIANT_DENSITY_ROWS   0x1u  /* density: one loop per cell row */
+#define SPH_VARIANT_XSPH_ROWS      0x2u  /* XSPH: one loop per cell row */
+#define SPH_VARIANT_FORCE_PREFETCH 0x4u  /* force: load the next neighbour early */
 typedef struct sph_exec_config {
     uint32_t tile;
     uint32_t persistent;
     float skin;
-    uint32_t pad_;
+    uint32_t variant;
 } sph_exec_config;
 int sph_set_exec(sph_system* s, const sph_exec_config* e);
 int sph_get_exec(const sph_system* s, sph_exec_config* e);

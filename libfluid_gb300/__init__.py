@@ -187,16 +187,16 @@ class FluidSystem:
     def setUseGraph(self, on: bool) -> None:
         self._ck(self._L.sph_set_use_graph(self._h, 1 if on else 0))
 
-    def setExec(self, tile: int = 256, persistent: int = 0, skin: float = 0.2) -> None:
+    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 3) -> None:
         from ._capi import SphExec
-        e = SphExec(tile, persistent, skin, 0)
+        e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_set_exec(self._h, C.byref(e)))
 
     def getExec(self) -> dict:
         from ._capi import SphExec
         e = SphExec()
         self._ck(self._L.sph_get_exec(self._h, C.byref(e)))
-        return {"tile": e.tile, "persistent": e.persistent, "skin": e.skin}
+        return {"tile": e.tile, "persistent": e.persistent, "skin": e.skin, "variant": e.variant}
 
     def setProfiling(self, on: bool) -> None:
         self._ck(self._L.sph_set_profiling(self._h, 1 if on else 0))

@@ -32,7 +32,13 @@ class SphParams(C.Structure):
 
 
 class SphExec(C.Structure):
-    _fields_ = [("tile", C.c_uint32), ("persistent", C.c_uint32), ("skin", C.c_float), ("pad_", C.c_uint32)]
+    _fields_ = [("tile", C.c_uint32), ("persistent", C.c_uint32), ("skin", C.c_float), ("variant", C.c_uint32)]
+
+
+# sph_exec_config.variant bits (include/sph_c.h)
+VARIANT_DENSITY_ROWS = 0x1
+VARIANT_XSPH_ROWS = 0x2
+VARIANT_FORCE_PREFETCH = 0x4
 
 
 class SphError(RuntimeError):

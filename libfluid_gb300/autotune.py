@@ -3,10 +3,12 @@
 Sweeps, on a GPU, the execution choices that do not change results (every
 choice computes bit-identical values; tests/test_exec_configs_gpu.py checks
 it): particles per tile (= threads per block), persistent blocks per SM for
-the neighbour passes (0 = one block per tile), and the neighbour-mask skin.
-Each candidate is timed with CUDA events over graph-replayed substeps after
-warm-up.  The best configuration per workload is written to tuned.json next
-to this file, which Batch and FluidSystem apply at creation.
+the neighbour passes (0 = one block per tile), the neighbour-mask skin, and
+then, on the best of those, the kernel-variant bits (per-row density and XSPH
+walks, force-kernel neighbour prefetch).  Each candidate is timed with CUDA
+events over graph-replayed substeps after warm-up.  The best configuration
+per workload is written to tuned.json next to this file; the engine's
+compiled-in defaults (ExecConfig in csrc/engine.h) follow that record.
 
     python -m libfluid_gb300.autotune [--workload batched|dam_break_1m|all] [--steps 20]
 """
@@ -24,6 +26,7 @@ TUNED = os.path.join(HERE, "tuned.json")
 TILES = (128, 256)
 PERSISTENT = (0, 2, 4)
 SKINS = (0.1, 0.15, 0.2, 0.3)
+VARIANTS = tuple(range(8))
 
 
 def load(workload: str) -> dict | None:
@@ -45,10 +48,10 @@ def _scenes(workload: str):
 
 
 def time_config(scenes, tile: int, persistent: int, skin: float, steps: int, warmup: int = 5,
-                device: int = 0) -> float:
+                device: int = 0, variant: int = 0) -> float:
     from .batch import Batch
     b = Batch(device)
-    b.set_exec(tile=tile, persistent=persistent, skin=skin)
+    b.set_exec(tile=tile, persistent=persistent, skin=skin, variant=variant)
     for s in scenes:
         b.add_scene(s)
     for _ in range(warmup):
@@ -70,12 +73,17 @@ def tune(workload: str, steps: int = 20, device: int = 0) -> dict:
     trials = []
     for tile, pers, skin in itertools.product(TILES, PERSISTENT, SKINS):
         ms = time_config(scenes, tile, pers, skin, steps, device=device)
-        trials.append({"tile": tile, "persistent": pers, "skin": skin, "ms_per_step": ms,
+        trials.append({"tile": tile, "persistent": pers, "skin": skin, "variant": 0, "ms_per_step": ms,
                        "particle_steps_per_s": n / (ms * 1e-3)})
+    best = min(trials, key=lambda t: t["ms_per_step"])
+    for v in VARIANTS[1:]:
+        ms = time_config(scenes, best["tile"], best["persistent"], best["skin"], steps, device=device, variant=v)
+        trials.append({"tile": best["tile"], "persistent": best["persistent"], "skin": best["skin"], "variant": v,
+                       "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3)})
     best = min(trials, key=lambda t: t["ms_per_step"])
     return {"workload": workload, "particles": n, "scenes": len(scenes), "steps": steps,
             "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
-            "best": {k: best[k] for k in ("tile", "persistent", "skin")}, "trials": trials}
+            "best": {k: best[k] for k in ("tile", "persistent", "skin", "variant")}, "trials": trials}
 
 
 def main():

@@ -131,9 +131,9 @@ class Batch:
     def set_use_graph(self, on: bool) -> None:
         self._ck(self._L.sph_batch_set_use_graph(self._h, 1 if on else 0))
 
-    def set_exec(self, tile: int = 256, persistent: int = 0, skin: float = 0.2) -> None:
+    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 3) -> None:
         from ._capi import SphExec
-        e = SphExec(tile, persistent, skin, 0)
+        e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_batch_set_exec(self._h, C.byref(e)))
 
     def timer_mark(self, slot: int) -> None:

@@ -378,6 +378,7 @@ int sph_set_exec(sph_system* s, const sph_exec_config* e) {
     x.tile = e->tile;
     x.persistent = e->persistent;
     x.skin = e->skin;
+    x.variant = e->variant;
     return eng_err(s, s->eng->set_exec(x));
 }
 int sph_get_exec(const sph_system* s, sph_exec_config* e) {
@@ -386,7 +387,7 @@ int sph_get_exec(const sph_system* s, sph_exec_config* e) {
     e->tile = x.tile;
     e->persistent = x.persistent;
     e->skin = x.skin;
-    e->pad_ = 0;
+    e->variant = x.variant;
     return SPH_OK;
 }
 int sph_set_profiling(sph_system* s, int on) {

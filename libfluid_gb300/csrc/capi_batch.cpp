@@ -132,6 +132,7 @@ int sph_batch_set_exec(sph_batch* b, const sph_exec_config* e) {
     x.tile = e->tile;
     x.persistent = e->persistent;
     x.skin = e->skin;
+    x.variant = e->variant;
     return berr(b, b->eng->set_exec(x));
 }
 int sph_batch_timer_mark(sph_batch* b, int slot) {

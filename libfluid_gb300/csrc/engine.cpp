@@ -293,6 +293,7 @@ int Engine::set_exec(const ExecConfig& e) {
     if (e.tile != 64 && e.tile != 128 && e.tile != 256) return fail(ENG_EINVAL, "tile must be 64, 128 or 256");
     if (!(e.skin > 0.0f && e.skin <= 1.0f)) return fail(ENG_EINVAL, "skin must be in (0, 1]");
     if (e.persistent > 64) return fail(ENG_EINVAL, "persistent blocks per SM must be <= 64");
+    if (e.variant & ~SPH_VARIANT_MASK) return fail(ENG_EINVAL, "unknown kernel variant bits");
     if (e.tile != exec_.tile) layout_dirty_ = true;
     graph_dirty_ = true;
     exec_ = e;
@@ -437,6 +438,8 @@ StepArgs Engine::args() const {
     a.block = exec_.tile;
     a.tile_ctr = exec_.persistent ? scal_ + 4 : nullptr;
     a.grid_nbr = exec_.persistent ? std::min<uint32_t>(a.ntiles, (uint32_t)sm_count_ * exec_.persistent) : a.ntiles;
+    a.variant = exec_.variant;
+    a.any_tension = any_tension_ ? 1u : 0u;
     a.dbg_nbr = debug_ ? dbg_nbr_ : nullptr;
     a.dbg_forces = debug_ ? dbg_forces_ : nullptr;
     return a;

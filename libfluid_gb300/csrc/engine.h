@@ -32,6 +32,7 @@ struct ExecConfig {
     uint32_t tile = 128;              // particles per tile = threads per block (64, 128 or 256)
     uint32_t persistent = 0;          // 0: one block per tile; k > 0: k blocks per SM pull tiles
     float skin = SPH_SKIN_DEFAULT;    // neighbour-mask skin (units of h)
+    uint32_t variant = SPH_VARIANT_DEFAULT;  // SPH_VARIANT_* bits
 };
 
 // Derive the device parameter block (FluidParams::setRes and setters,

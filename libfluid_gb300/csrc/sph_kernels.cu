@@ -213,8 +213,12 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 }
 
 // ---------------------------------------------------------------------------
-// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84).
+// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84).  ROWS selects
+// one candidate loop per (y,z) row with two loads in flight (true) or one
+// loop flattened across the rows (false); the candidates and their order are
+// the same.
 // ---------------------------------------------------------------------------
+template <bool ROWS>
 __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restrict__ params,
                                                       const DevScene* __restrict__ scenes,
                                                       const uint4* __restrict__ tiles,
@@ -243,32 +247,15 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
     // passes: mask words 0-8 hold the candidates within the skin radius
     // (XSPH), words 9-17 the exact neighbours j != i, eps < r^2 <= h^2 (the
     // normal and force passes' test, evaluated bit for bit the same way).
-    // One loop runs across all 9 rows so lanes do not wait at row ends.
-    int r = -1;
-    uint32_t jb = 0, j = 0, je = 0, bs = 0u, be = 0u;
-    bool valid = false;
-    for (;;) {
-        if (j >= je) {
-            if (valid) {
-                mask[(size_t)r * mask_stride + k] = bs;
-                mask[(size_t)(9 + r) * mask_stride + k] = be;
-            }
-            if (++r >= 9) break;
-            bs = be = 0u;
-            valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
-            if (!valid) jb = je = 0;
-            j = jb;
-            continue;
-        }
-        const float4 q = __ldg(P1 + j);
+    auto visit = [&](const float4& q, uint32_t jj, uint32_t jb0, uint32_t& bs0, uint32_t& be0) {
         const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
-        if (rr <= skin2 && j != k) {
-            const uint32_t off = j - jb;
+        if (rr <= skin2 && jj != k) {
+            const uint32_t off = jj - jb0;
             const uint32_t bit = (off < 32u) ? (1u << off) : 0u;
-            bs |= bit;
+            bs0 |= bit;
             if (rr <= h2) {
-                if (rr > eps) be |= bit;
+                if (rr > eps) be0 |= bit;
                 const float rd = sqrtf(rr);
                 const float x = fmaf(-rd, rd, h2);
                 const float w = (rd >= h) ? 0.0f : c6 * (x * x * x);
@@ -276,7 +263,44 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
                 cnt++;
             }
         }
-        ++j;
+    };
+    if (ROWS) {
+#pragma unroll 1
+        for (int rr = 0; rr < 9; ++rr) {
+            uint32_t jb0, je0, bs0 = 0u, be0 = 0u;
+            if (row_range(pp, start, sc.cell_base, delta, g, rr, jb0, je0)) {
+                uint32_t jj = jb0;
+                for (; jj + 2u <= je0; jj += 2u) {
+                    const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
+                    visit(q0, jj, jb0, bs0, be0);
+                    visit(q1, jj + 1u, jb0, bs0, be0);
+                }
+                if (jj < je0) visit(__ldg(P1 + jj), jj, jb0, bs0, be0);
+                mask[(size_t)rr * mask_stride + k] = bs0;
+                mask[(size_t)(9 + rr) * mask_stride + k] = be0;
+            }
+        }
+    } else {
+        // one loop across all 9 rows, so lanes do not wait at row ends
+        int r = -1;
+        uint32_t jb = 0, j = 0, je = 0, bs = 0u, be = 0u;
+        bool valid = false;
+        for (;;) {
+            if (j >= je) {
+                if (valid) {
+                    mask[(size_t)r * mask_stride + k] = bs;
+                    mask[(size_t)(9 + r) * mask_stride + k] = be;
+                }
+                if (++r >= 9) break;
+                bs = be = 0u;
+                valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
+                if (!valid) jb = je = 0;
+                j = jb;
+                continue;
+            }
+            visit(__ldg(P1 + j), j, jb, bs, be);
+            ++j;
+        }
     }
     const float d = fabsf(sdf_box(pp, p.x, p.y, p.z));
     float corr = sum;
@@ -349,8 +373,12 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
 // force buffers in the reference's order, which after the swapped arguments
 // at fluidsystem.cu:352-364 is ((pressure + tension) + viscosity) + adhesion.
 // ---------------------------------------------------------------------------
+// TENSION = false is the build for launches where no scene has surface
+// tension (the tension terms are then compiled out); PREFETCH issues the next
+// neighbour's position load before the current pair is evaluated.
 // (256 threads, 3 blocks per SM: ptxas keeps it at 79 registers without spills;
 // with the default heuristic it caps at 64 and spills)
+template <bool TENSION, bool PREFETCH>
 __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams* __restrict__ params,
                                                               const DevScene* __restrict__ scenes,
                                                               const uint4* __restrict__ tiles,
@@ -376,7 +404,7 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
     const float4 vi = V1[k];
     const float4 si = S[k];
     const int3 g = grid_of(pp, pi.x, pi.y, pi.z);
-    const bool tension = (pp.flags & 1u) != 0u;
+    const bool tension = TENSION && (pp.flags & 1u) != 0u;
     float fpx = 0.f, fpy = 0.f, fpz = 0.f;   // pressure
     float fvx = 0.f, fvy = 0.f, fvz = 0.f;   // "viscosity" (pressure re-added)
     float ftx = 0.f, fty = 0.f, ftz = 0.f;   // tension
@@ -386,12 +414,24 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
         const float ri = si.x, pri = si.y, csi = si.z;
         float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
         if (tension) ni = N[k];
+        (void)ni;
         const float h2 = pp.h2, eps = pp.eps, inv_ri2 = si.w;
         // exact neighbours recorded by the density pass (mask words 9-17)
         MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
-        uint32_t j;
-        while (walk.next(j)) {
-            const float4 pj = __ldg(P1 + j);
+        uint32_t j = 0, jn = 0;
+        bool has = walk.next(j);
+        float4 pnext = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (PREFETCH && has) pnext = __ldg(P1 + j);
+        while (has) {
+            float4 pj;
+            if (PREFETCH) {
+                pj = pnext;
+                const bool hn = walk.next(jn);
+                if (hn) pnext = __ldg(P1 + jn);
+                has = hn;
+            } else {
+                pj = __ldg(P1 + j);
+            }
             const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
             if (r2 <= h2 && r2 > eps && j != k) {
@@ -430,6 +470,8 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
                     }
                 }
             }
+            if (PREFETCH) j = jn;
+            else has = walk.next(j);
         }
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
         ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
@@ -516,7 +558,11 @@ __device__ __forceinline__ void xsph_pair(const float4* __restrict__ P0, const f
 // reference updates velocities in place while neighbours read them (a race);
 // here reads see V2 and the result goes to V0 (Jacobi).
 // ---------------------------------------------------------------------------
+// ROWS selects the candidate walk: one loop per (y,z) row (true) or one loop
+// flattened across the rows (false); both visit the same candidates in the
+// same order.
 // (no __launch_bounds__: with it ptxas caps this kernel at 48 registers and spills)
+template <bool ROWS>
 __global__ void k_xsph(const DevParams* __restrict__ params,
                                                    const DevScene* __restrict__ scenes,
                                                    const uint4* __restrict__ tiles,
@@ -547,7 +593,12 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
     // positions; a pair can close to h after the move only if the particles
     // moved less than skin*h/2 each, which the force pass recorded.
     uint32_t j;
-    if (__uint_as_float(__ldg(maxdisp)) <= pp.xsph_disp_limit2) {
+    const bool masked = __uint_as_float(__ldg(maxdisp)) <= pp.xsph_disp_limit2;
+    if (ROWS) {
+        auto visit = [&](uint32_t jj) { xsph_pair(P0, V2, jj, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz); };
+        if (masked) for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, visit);   // skin words 0-8
+        else for_candidates(pp, start, sc.cell_base, delta, g, visit);
+    } else if (masked) {
         MaskWalk walk(pp, start, sc.cell_base, delta, g, mask, mask_stride, k);   // skin mask, words 0-8
         while (walk.next(j)) xsph_pair(P0, V2, j, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz);
     } else {
@@ -668,8 +719,9 @@ cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
-    k_density<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask,
-                                              a.mask_stride, a.dbg_nbr, a.ntiles, ctr(a, 0));
+    auto kern = (a.variant & SPH_VARIANT_DENSITY_ROWS) ? k_density<true> : k_density<false>;
+    kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
+                                         a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
 }
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
@@ -678,14 +730,18 @@ cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
-    k_force_integrate<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S,
-                                                      a.N, a.mask, a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp,
-                                                      a.dbg_forces, a.ntiles, ctr(a, 2));
+    const bool pre = (a.variant & SPH_VARIANT_FORCE_PREFETCH) != 0u;
+    auto kern = a.any_tension ? (pre ? k_force_integrate<true, true> : k_force_integrate<true, false>)
+                              : (pre ? k_force_integrate<false, true> : k_force_integrate<false, false>);
+    kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S, a.N, a.mask,
+                                         a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp, a.dbg_forces, a.ntiles,
+                                         ctr(a, 2));
     return cudaGetLastError();
 }
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st) {
-    k_xsph<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.mask,
-                                           a.mask_stride, a.maxdisp, a.V0, a.ntiles, ctr(a, 3));
+    auto kern = (a.variant & SPH_VARIANT_XSPH_ROWS) ? k_xsph<true> : k_xsph<false>;
+    kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.mask,
+                                         a.mask_stride, a.maxdisp, a.V0, a.ntiles, ctr(a, 3));
     return cudaGetLastError();
 }
 cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,

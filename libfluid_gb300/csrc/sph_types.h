@@ -44,6 +44,15 @@ struct DevParams {
 // the device; otherwise XSPH walks all candidates).
 #define SPH_SKIN_DEFAULT 0.1f
 
+// Kernel variants (bits of the execution config's `variant`). All variants
+// visit neighbours in the same order and give identical results; they differ
+// only in how the walk is scheduled.
+#define SPH_VARIANT_DENSITY_ROWS  0x1u   // density: one loop per cell row, two loads in flight
+#define SPH_VARIANT_XSPH_ROWS     0x2u   // XSPH: one loop per cell row instead of one flattened walk
+#define SPH_VARIANT_FORCE_PREFETCH 0x4u  // force: load the next neighbour before the current pair
+#define SPH_VARIANT_MASK          0x7u
+#define SPH_VARIANT_DEFAULT       0x3u   // measured fastest on the 1M dam break and the 256-scene batch
+
 // Scene placement in the engine's arenas.
 struct DevScene {
     uint32_t part_base;   // first particle slot of the scene
