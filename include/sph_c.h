@@ -135,6 +135,30 @@ int sph_get_derived(const sph_system* s, double* out, int cap);
 /* The same derivation for a parameter set, without a device (host only). */
 int sph_derive_params(const sph_params* p, double* out, int cap);
 
+/* ---- snapshot / resume ---------------------------------------------------
+ * No counterpart in the reference (it has no checkpointing).  A snapshot is
+ * a 128-byte header (magic, version, particle count, the parameter set in
+ * force) followed by positions, velocities and accelerations of every
+ * particle as 4 floats each (xyz and the slot's w lane), in the current
+ * slot order: sph_snapshot_bytes(n) = 128 + 48 n bytes, little endian.
+ * Restoring into a system holding the same particle count (any parameters)
+ * replaces its parameters and state; stepping then continues bit for bit as
+ * the snapshotted system would have.  Errors: SPH_EINVAL for a short
+ * buffer, a bad magic/version or a particle-count mismatch. */
+#define SPH_SNAPSHOT_MAGIC 0x53485053u   /* "SPHS" */
+#define SPH_SNAPSHOT_VERSION 1u
+typedef struct sph_snapshot_header {
+    uint32_t magic;
+    uint32_t version;
+    uint32_t n;
+    uint32_t header_bytes;   /* 128 */
+    sph_params params;
+    uint32_t reserved[6];
+} sph_snapshot_header;
+uint64_t sph_snapshot_bytes(uint32_t n);
+int sph_snapshot(sph_system* s, void* buf, uint64_t cap, uint64_t* written);
+int sph_restore(sph_system* s, const void* buf, uint64_t bytes);
+
 /* ---- parity / debug taps ----------------------------------------------- */
 /* Per-particle and per-cell intermediates of the last substep, indexed like
  * the reference's device vectors after that substep (cell order). */
@@ -167,10 +191,10 @@ int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
  * blocks per SM taking tiles from a counter in the neighbour passes; skin:
  * neighbour-mask skin in units of h, in (0, 1]; variant: SPH_VARIANT_* bits
  * choosing how the neighbour walks are scheduled.  Defaults: tile 128,
- * persistent 0, skin 0.1, variant 3 (per-row density and XSPH walks). */
+ * persistent 0, skin 0.1, variant 7 (per-row walks, 64-register force build). */
 #define SPH_VARIANT_DENSITY_ROWS   0x1u  /* density: one loop per cell row */
 #define SPH_VARIANT_XSPH_ROWS      0x2u  /* XSPH: one loop per cell row */
-#define SPH_VARIANT_FORCE_PREFETCH 0x4u  /* force: load the next neighbour early */
+#define SPH_VARIANT_FORCE_OCC      0x4u  /* force: 64-register build, more resident warps */
 typedef struct sph_exec_config {
     uint32_t tile;
     uint32_t persistent;
@@ -229,6 +253,9 @@ int sph_batch_step(sph_batch* b, uint32_t substeps);
 int sph_batch_step_async(sph_batch* b, uint32_t substeps);
 int sph_batch_sync(sph_batch* b);
 int sph_batch_get_state(sph_batch* b, int scene_id, float* pos, float* colour, float* vel, uint32_t n);
+/* Snapshot / resume of one scene, in the sph_snapshot format (above). */
+int sph_batch_snapshot(sph_batch* b, int scene_id, void* buf, uint64_t cap, uint64_t* written);
+int sph_batch_restore(sph_batch* b, int scene_id, const void* buf, uint64_t bytes);
 uint32_t sph_batch_num_scenes(const sph_batch* b);
 uint64_t sph_batch_num_particles(const sph_batch* b);
 int sph_batch_debug_enable(sph_batch* b, int on);

@@ -125,6 +125,20 @@ class FluidSystem:
         self._ck(self._L.sph_get_pscale(self._h, C.byref(out)))
         return out.value
 
+    # ---- snapshot / resume (no reference counterpart) ----------------------
+    def snapshot(self) -> bytes:
+        """Exact snapshot (header + positions, velocities, accelerations)."""
+        n = self.numParticles()
+        size = int(self._L.sph_snapshot_bytes(n))
+        buf = C.create_string_buffer(size)
+        written = C.c_uint64(0)
+        self._ck(self._L.sph_snapshot(self._h, buf, size, C.byref(written)))
+        return buf.raw[:written.value]
+
+    def restore(self, snap: bytes) -> None:
+        """Replace parameters and state with a snapshot of the same particle count."""
+        self._ck(self._L.sph_restore(self._h, snap, len(snap)))
+
     # ---- setters (fluidsystem.cu:412-475) ---------------------------------
     def setRestDensity(self, v: float) -> None: self._ck(self._L.sph_set_rest_density(self._h, v))
     def setParticleSize(self, v: float) -> None: self._ck(self._L.sph_set_particle_size(self._h, v))
@@ -187,7 +201,7 @@ class FluidSystem:
     def setUseGraph(self, on: bool) -> None:
         self._ck(self._L.sph_set_use_graph(self._h, 1 if on else 0))
 
-    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 3) -> None:
+    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 7) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_set_exec(self._h, C.byref(e)))

@@ -38,7 +38,7 @@ class SphExec(C.Structure):
 # sph_exec_config.variant bits (include/sph_c.h)
 VARIANT_DENSITY_ROWS = 0x1
 VARIANT_XSPH_ROWS = 0x2
-VARIANT_FORCE_PREFETCH = 0x4
+VARIANT_FORCE_OCC = 0x4
 
 
 class SphError(RuntimeError):
@@ -73,6 +73,9 @@ SIGNATURES = [
     ("sph_get_pscale", _I, [_P, _FP]),
     ("sph_num_particles", _U32, [_P]),
     ("sph_is_init", _I, [_P]),
+    ("sph_snapshot_bytes", C.c_uint64, [_U32]),
+    ("sph_snapshot", _I, [_P, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("sph_restore", _I, [_P, _P, C.c_uint64]),
     ("sph_set_rest_density", _I, [_P, _F]),
     ("sph_set_particle_size", _I, [_P, _F]),
     ("sph_set_gas_constant", _I, [_P, _F]),

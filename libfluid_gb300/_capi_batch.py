@@ -24,6 +24,8 @@ SIGNATURES = [
     ("sph_batch_step_async", _I, [_P, _U32]),
     ("sph_batch_sync", _I, [_P]),
     ("sph_batch_get_state", _I, [_P, _I, _P, _P, _P, _U32]),
+    ("sph_batch_snapshot", _I, [_P, _I, _P, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("sph_batch_restore", _I, [_P, _I, _P, C.c_uint64]),
     ("sph_batch_num_scenes", _U32, [_P]),
     ("sph_batch_num_particles", C.c_uint64, [_P]),
     ("sph_batch_debug_enable", _I, [_P, _I]),

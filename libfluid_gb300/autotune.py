@@ -5,7 +5,7 @@ choice computes bit-identical values; tests/test_exec_configs_gpu.py checks
 it): particles per tile (= threads per block), persistent blocks per SM for
 the neighbour passes (0 = one block per tile), the neighbour-mask skin, and
 then, on the best of those, the kernel-variant bits (per-row density and XSPH
-walks, force-kernel neighbour prefetch).  Each candidate is timed with CUDA
+walks, the force kernel's register budget).  Each candidate is timed with CUDA
 events over graph-replayed substeps after warm-up.  The best configuration
 per workload is written to tuned.json next to this file; the engine's
 compiled-in defaults (ExecConfig in csrc/engine.h) follow that record.

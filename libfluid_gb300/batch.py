@@ -103,6 +103,17 @@ class Batch:
         self._ck(self._L.sph_batch_get_state(self._h, sid, *[o.ctypes.data for o in outs], n))
         return tuple(outs)
 
+    def snapshot(self, sid: int) -> bytes:
+        """Exact snapshot of one scene (sph_snapshot format)."""
+        size = int(self._L.sph_snapshot_bytes(self.scenes[sid].n))
+        buf = C.create_string_buffer(size)
+        written = C.c_uint64(0)
+        self._ck(self._L.sph_batch_snapshot(self._h, sid, buf, size, C.byref(written)))
+        return buf.raw[:written.value]
+
+    def restore(self, sid: int, snap: bytes) -> None:
+        self._ck(self._L.sph_batch_restore(self._h, sid, snap, len(snap)))
+
     @property
     def num_scenes(self) -> int:
         return int(self._L.sph_batch_num_scenes(self._h))
@@ -131,7 +142,7 @@ class Batch:
     def set_use_graph(self, on: bool) -> None:
         self._ck(self._L.sph_batch_set_use_graph(self._h, 1 if on else 0))
 
-    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 3) -> None:
+    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 7) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_batch_set_exec(self._h, C.byref(e)))

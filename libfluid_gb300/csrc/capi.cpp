@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "snapshot_fmt.h"
 
 using sph::Engine;
 using sph::SceneConfig;
@@ -246,6 +247,37 @@ int sph_get_pscale(const sph_system* s, float* out) {
 }
 uint32_t sph_num_particles(const sph_system* s) { return s ? s->n : 0; }
 int sph_is_init(const sph_system* s) { return (s && s->is_init) ? 1 : 0; }
+
+uint64_t sph_snapshot_bytes(uint32_t n) { return sph::snapshot_total_bytes(n); }
+
+int sph_snapshot(sph_system* s, void* buf, uint64_t cap, uint64_t* written) {
+    if (!s || !buf) return SPH_EINVAL;
+    if (!s->is_init) return set_err(s, SPH_ENOTINIT, "snapshot before init");
+    const uint64_t need = sph::snapshot_total_bytes(s->n);
+    if (cap < need) return set_err(s, SPH_EINVAL, "snapshot buffer smaller than sph_snapshot_bytes(n)");
+    sph_params p;
+    sph_get_params(s, &p);
+    sph_snapshot_header h;
+    sph::snapshot_make_header(h, s->n, p);
+    std::memcpy(buf, &h, sizeof(h));
+    float4* body = reinterpret_cast<float4*>(static_cast<char*>(buf) + sizeof(h));
+    int rc = eng_err(s, s->eng->save_state(s->scene, body, s->n));
+    if (rc == SPH_OK && written) *written = need;
+    return rc;
+}
+
+int sph_restore(sph_system* s, const void* buf, uint64_t bytes) {
+    if (!s || !buf) return SPH_EINVAL;
+    if (!s->is_init) return set_err(s, SPH_ENOTINIT, "restore before init");
+    sph_snapshot_header h;
+    std::string why;
+    if (!sph::snapshot_parse(buf, bytes, &h, &why)) return set_err(s, SPH_EINVAL, why);
+    if (h.n != s->n) return set_err(s, SPH_EINVAL, "snapshot particle count differs from the system's");
+    int rc = sph_set_params(s, &h.params);
+    if (rc) return rc;
+    const float4* body = reinterpret_cast<const float4*>(static_cast<const char*>(buf) + sizeof(h));
+    return eng_err(s, s->eng->load_state(s->scene, body, s->n));
+}
 
 #define SPH_SETTER(name, field)                     \
     int name(sph_system* s, float v) {              \

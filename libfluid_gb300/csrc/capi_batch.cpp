@@ -6,6 +6,7 @@
 
 #include "../../include/sph_c.h"
 #include "engine.h"
+#include "snapshot_fmt.h"
 
 using sph::Engine;
 using sph::SceneConfig;
@@ -35,6 +36,19 @@ bool to_config(const sph_params* p, SceneConfig& c, std::string* err) {
     c.gravity[0] = p->gravity[0]; c.gravity[1] = p->gravity[1]; c.gravity[2] = p->gravity[2];
     DevParams dp;
     return sph::derive_params(c, dp, err);
+}
+
+void from_config(const SceneConfig& c, sph_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->box_mode = (uint32_t)c.box_mode;
+    p->res = c.res;
+    p->lx = c.lx; p->ly = c.ly; p->lz = c.lz; p->h = c.h;
+    p->rest_density = c.rest_density; p->gas_constant = c.gas_constant; p->gamma = c.gamma;
+    p->mass = c.mass; p->particle_size = c.particle_size;
+    p->xsph = c.xsph; p->surface_tension = c.surface_tension; p->viscosity = c.viscosity;
+    p->adhesion = c.adhesion; p->vdamp = c.vdamp;
+    p->vel_limit = c.vel_limit; p->acc_limit = c.acc_limit; p->dt = c.dt;
+    p->gravity[0] = c.gravity[0]; p->gravity[1] = c.gravity[1]; p->gravity[2] = c.gravity[2];
 }
 
 }  // namespace
@@ -108,6 +122,36 @@ int sph_batch_sync(sph_batch* b) {
 int sph_batch_get_state(sph_batch* b, int scene_id, float* pos, float* colour, float* vel, uint32_t n) {
     if (!b) return SPH_EINVAL;
     return berr(b, b->eng->get_state(scene_id, pos, colour, vel, n));
+}
+
+int sph_batch_snapshot(sph_batch* b, int scene_id, void* buf, uint64_t cap, uint64_t* written) {
+    if (!b || !buf) return SPH_EINVAL;
+    const sph::Scene* sc = b->eng->scene(scene_id);
+    if (!sc) { b->err = "unknown scene id"; return SPH_EINVAL; }
+    const uint64_t need = sph::snapshot_total_bytes(sc->n);
+    if (cap < need) { b->err = "snapshot buffer smaller than sph_snapshot_bytes(n)"; return SPH_EINVAL; }
+    sph_params p;
+    from_config(sc->cfg, &p);
+    sph_snapshot_header h;
+    sph::snapshot_make_header(h, sc->n, p);
+    std::memcpy(buf, &h, sizeof(h));
+    float4* body = reinterpret_cast<float4*>(static_cast<char*>(buf) + sizeof(h));
+    int rc = berr(b, b->eng->save_state(scene_id, body, sc->n));
+    if (rc == SPH_OK && written) *written = need;
+    return rc;
+}
+
+int sph_batch_restore(sph_batch* b, int scene_id, const void* buf, uint64_t bytes) {
+    if (!b || !buf) return SPH_EINVAL;
+    const sph::Scene* sc = b->eng->scene(scene_id);
+    if (!sc) { b->err = "unknown scene id"; return SPH_EINVAL; }
+    sph_snapshot_header h;
+    if (!sph::snapshot_parse(buf, bytes, &h, &b->err)) return SPH_EINVAL;
+    if (h.n != sc->n) { b->err = "snapshot particle count differs from the scene's"; return SPH_EINVAL; }
+    int rc = sph_batch_set_params(b, scene_id, &h.params);
+    if (rc) return rc;
+    const float4* body = reinterpret_cast<const float4*>(static_cast<const char*>(buf) + sizeof(h));
+    return berr(b, b->eng->load_state(scene_id, body, h.n));
 }
 
 uint32_t sph_batch_num_scenes(const sph_batch* b) { return b ? (uint32_t)b->eng->num_scenes() : 0; }

@@ -639,6 +639,37 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     return ENG_OK;
 }
 
+int Engine::save_state(int id, float4* host, uint32_t n) {
+    cudaSetDevice(device_);
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
+    if (n == 0) return ENG_OK;
+    const size_t bytes = (size_t)n * sizeof(float4);
+    ENG_CK(cudaMemcpyAsync(host, P0_ + s->part_base, bytes, cudaMemcpyDeviceToHost, stream_), "snapshot");
+    ENG_CK(cudaMemcpyAsync(host + n, V0_ + s->part_base, bytes, cudaMemcpyDeviceToHost, stream_), "snapshot");
+    ENG_CK(cudaMemcpyAsync(host + 2 * (size_t)n, A0_ + s->part_base, bytes, cudaMemcpyDeviceToHost, stream_),
+           "snapshot");
+    ENG_CK(cudaStreamSynchronize(stream_), "snapshot sync");
+    return ENG_OK;
+}
+
+int Engine::load_state(int id, const float4* host, uint32_t n) {
+    cudaSetDevice(device_);
+    const Scene* s = scene(id);
+    if (!s) return fail(ENG_EINVAL, "unknown scene id");
+    if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
+    if (n == 0) return ENG_OK;
+    const size_t bytes = (size_t)n * sizeof(float4);
+    ENG_CK(cudaMemcpyAsync(P0_ + s->part_base, host, bytes, cudaMemcpyHostToDevice, stream_), "restore");
+    ENG_CK(cudaMemcpyAsync(V0_ + s->part_base, host + n, bytes, cudaMemcpyHostToDevice, stream_), "restore");
+    ENG_CK(cudaMemcpyAsync(A0_ + s->part_base, host + 2 * (size_t)n, bytes, cudaMemcpyHostToDevice, stream_),
+           "restore");
+    ENG_CK(cudaMemsetAsync(S_ + s->part_base, 0, bytes, stream_), "restore");
+    ENG_CK(cudaStreamSynchronize(stream_), "restore sync");
+    return ENG_OK;
+}
+
 int Engine::debug_enable(bool on) {
     if (on == debug_) return ENG_OK;
     debug_ = on;

@@ -68,6 +68,10 @@ public:
     int set_positions(int id, uint32_t first, const float* pos, uint32_t count);
     int generate_lattice(int id, const LatticeSpec& spec, uint32_t first);
     int get_state(int id, float* pos, float* colour, float* vel, uint32_t n, bool to_device = false);
+    // Exact state (3n float4 on the host: positions, velocities,
+    // accelerations, in slot order, w lanes included) for snapshot/resume.
+    int save_state(int id, float4* host, uint32_t n);
+    int load_state(int id, const float4* host, uint32_t n);
 
     // Advance every live scene by `substeps` substeps (all with their own dt).
     int step(uint32_t substeps, bool sync = true);

@@ -345,20 +345,22 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
     float sx = 0.f, sy = 0.f, sz = 0.f;
     MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
     uint32_t j;
+    // m gradPoly6(r) rvec / (rho_j r) = m c (h^2 - r^2)^2 rvec / rho_j: the
+    // factor r of gradPoly6 cancels the 1/r; h^2 - r^2 is formed from the
+    // rounded root r as gradPoly6 forms it (it cancels near r = h)
+    const float mc = pp.mass * pp.grad_poly6;
     while (walk.next(j)) {
         const float4 q = __ldg(P1 + j);
+        const float rhoj = __ldg(&S[j].x);
         const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
         const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (r2 <= pp.h2 && r2 > pp.eps && j != k) {
-            const float rhoj = __ldg(&S[j].x);
-            if (rhoj > pp.eps) {
-                const float r = sqrtf(r2);
-                const float s = pp.mass * grad_poly6(pp, r);
-                const float den = rhoj * r;
-                sx = sx + (s * rx) / den;
-                sy = sy + (s * ry) / den;
-                sz = sz + (s * rz) / den;
-            }
+        if (r2 <= pp.h2 && r2 > pp.eps && j != k && rhoj > pp.eps) {
+            const float r = sqrtf(r2);
+            const float x = fmaf(-r, r, pp.h2);
+            const float s = (r >= pp.h) ? 0.0f : __fdividef(mc * (x * x), rhoj);
+            sx = fmaf(s, rx, sx);
+            sy = fmaf(s, ry, sy);
+            sz = fmaf(s, rz, sz);
         }
     }
     N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
@@ -374,12 +376,13 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
 // at fluidsystem.cu:352-364 is ((pressure + tension) + viscosity) + adhesion.
 // ---------------------------------------------------------------------------
 // TENSION = false is the build for launches where no scene has surface
-// tension (the tension terms are then compiled out); PREFETCH issues the next
-// neighbour's position load before the current pair is evaluated.
-// (256 threads, 3 blocks per SM: ptxas keeps it at 79 registers without spills;
-// with the default heuristic it caps at 64 and spills)
-template <bool TENSION, bool PREFETCH>
-__global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams* __restrict__ params,
+// tension (the tension terms are then compiled out).  MINB is the register
+// budget as resident blocks of 256 threads per SM: 3 (85 registers; the
+// tension-free build needs 72, the tension build 80, no spills) or 4 (64
+// registers, more warps per SM, a few spilled values).
+template <bool TENSION, int MINB>
+__global__ void __launch_bounds__(SPH_TILE, MINB)
+k_force_integrate(const DevParams* __restrict__ params,
                                                               const DevScene* __restrict__ scenes,
                                                               const uint4* __restrict__ tiles,
                                                               const uint32_t* __restrict__ start,
@@ -414,64 +417,54 @@ __global__ void __launch_bounds__(SPH_TILE, 3) k_force_integrate(const DevParams
         const float ri = si.x, pri = si.y, csi = si.z;
         float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
         if (tension) ni = N[k];
-        (void)ni;
         const float h2 = pp.h2, eps = pp.eps, inv_ri2 = si.w;
         // exact neighbours recorded by the density pass (mask words 9-17)
         MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
-        uint32_t j = 0, jn = 0;
-        bool has = walk.next(j);
-        float4 pnext = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (PREFETCH && has) pnext = __ldg(P1 + j);
-        while (has) {
-            float4 pj;
-            if (PREFETCH) {
-                pj = pnext;
-                const bool hn = walk.next(jn);
-                if (hn) pnext = __ldg(P1 + jn);
-                has = hn;
-            } else {
-                pj = __ldg(P1 + j);
-            }
+        // 2 rho0 / (rho_i + rho_i) of the tension sum (fluidphysics.cu:293), once per particle
+        const float tden = (2.0f * pp.rest_density) / (ri + ri);
+        const float sm = -pp.surface_tension * pp.mass;
+        const float coh_m = -pp.mass * pp.mass;
+        uint32_t j;
+        while (walk.next(j)) {
+            // The mask holds exact neighbours, so position, (rho, p, c^2, 1/rho^2)
+            // and velocity of nearly every j are needed: the loads are issued
+            // together, before any test, so their latencies overlap.
+            const float4 pj = __ldg(P1 + j), sj = __ldg(S + j), vj = __ldg(V1 + j);
+            float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (tension) nj = __ldg(N + j);
             const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-            if (r2 <= h2 && r2 > eps && j != k) {
-                const float4 sj = __ldg(S + j);
-                if (sj.x > eps) {
-                    const float4 vj = __ldg(V1 + j);
-                    const float r = sqrtf(r2);
-                    const float inv_r = 1.0f / r;
-                    const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
-                    // artificial viscosity, only for approaching pairs; evaluated
-                    // without a branch (finite for every pair) and selected
-                    const float mu = (pp.h * ux) / (r2 + pp.visc_eps);
-                    const float Pv = (-pp.viscosity * (csi + sj.z) * mu) / (ri + sj.x);
-                    const float Pi = (ux < 0.0f) ? Pv : 0.0f;
-                    // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
-                    const float mid = sj.y * inv_ri2 + pri * sj.w;
-                    const float s = pp.mass * grad_spiky(pp, r);
-                    const float cx = (s * rx) * inv_r, cy = (s * ry) * inv_r, cz = (s * rz) * inv_r;
-                    fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
-                    const float mp = mid + Pi;
-                    fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
-                    if (tension) {
-                        // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
-                        // sigma == 0 the tension force is sigma * (finite sum) = 0, so
-                        // the term is skipped.
-                        const float sc2 = -pp.mass * pp.mass * cohesion_k(pp, r);
-                        const float hx = (sc2 * rx) * inv_r, hy = (sc2 * ry) * inv_r, hz = (sc2 * rz) * inv_r;
-                        const float4 nj = __ldg(N + j);
-                        const float sm = -pp.surface_tension * pp.mass;
-                        const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
-                        const float tr = 2.0f * pp.rest_density;
-                        const float den = ri + ri;
-                        ftx = ftx + (tr * (hx + kx)) / den;
-                        fty = fty + (tr * (hy + ky)) / den;
-                        ftz = ftz + (tr * (hz + kz)) / den;
-                    }
+            if (r2 <= h2 && r2 > eps && j != k && sj.x > eps) {
+                // r is the correctly rounded root: h - r below cancels, and pairs at
+                // r ~ h must see the reference's r; 1/r only scales (approximate)
+                const float r = sqrtf(r2);
+                const float inv_r = rsqrtf(r2);
+                const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
+                // artificial viscosity -visc (cs_i + cs_j) mu / (rho_i + rho_j),
+                // mu = h ux / (r^2 + 0.01 h^2), only for approaching pairs;
+                // evaluated without a branch (finite for every pair) and selected
+                const float Pv = __fdividef(-pp.viscosity * (csi + sj.z) * (pp.h * ux),
+                                            (r2 + pp.visc_eps) * (ri + sj.x));
+                const float Pi = (ux < 0.0f) ? Pv : 0.0f;
+                // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
+                const float mid = sj.y * inv_ri2 + pri * sj.w;
+                const float sr = (pp.mass * grad_spiky(pp, r)) * inv_r;
+                const float cx = sr * rx, cy = sr * ry, cz = sr * rz;
+                fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
+                const float mp = mid + Pi;
+                fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
+                if (tension) {
+                    // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
+                    // sigma == 0 the tension force is sigma * (finite sum) = 0, so
+                    // the term is skipped.
+                    const float sc2 = coh_m * cohesion_k(pp, r) * inv_r;
+                    const float hx = sc2 * rx, hy = sc2 * ry, hz = sc2 * rz;
+                    const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
+                    ftx = fmaf(tden, hx + kx, ftx);
+                    fty = fmaf(tden, hy + ky, fty);
+                    ftz = fmaf(tden, hz + kz, ftz);
                 }
             }
-            if (PREFETCH) j = jn;
-            else has = walk.next(j);
         }
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
         ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
@@ -537,6 +530,7 @@ __device__ __forceinline__ void xsph_pair(const float4* __restrict__ P0, const f
                                           uint32_t k, const float4& pi, const float4& vi, float h2, float h, float c6,
                                           float two_m, float eps, float& sx, float& sy, float& sz) {
     const float4 q = __ldg(P0 + j);
+    const float4 vj = __ldg(V2 + j);   // issued with the position: most candidates are neighbours
     const float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
     const float rr = dot3(dx, dy, dz, dx, dy, dz);
     const float rs = pi.w + q.w;
@@ -544,8 +538,7 @@ __device__ __forceinline__ void xsph_pair(const float4* __restrict__ P0, const f
         const float r = sqrtf(rr);
         const float x = fmaf(-r, r, h2);
         const float w = (r >= h) ? 0.0f : c6 * (x * x * x);
-        const float coeff = w * (two_m / rs);
-        const float4 vj = __ldg(V2 + j);
+        const float coeff = w * __fdividef(two_m, rs);
         sx = fmaf(coeff, vj.x - vi.x, sx);
         sy = fmaf(coeff, vj.y - vi.y, sy);
         sz = fmaf(coeff, vj.z - vi.z, sz);
@@ -730,9 +723,9 @@ cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
-    const bool pre = (a.variant & SPH_VARIANT_FORCE_PREFETCH) != 0u;
-    auto kern = a.any_tension ? (pre ? k_force_integrate<true, true> : k_force_integrate<true, false>)
-                              : (pre ? k_force_integrate<false, true> : k_force_integrate<false, false>);
+    const bool occ = (a.variant & SPH_VARIANT_FORCE_OCC) != 0u;
+    auto kern = a.any_tension ? (occ ? k_force_integrate<true, 4> : k_force_integrate<true, 3>)
+                              : (occ ? k_force_integrate<false, 4> : k_force_integrate<false, 3>);
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S, a.N, a.mask,
                                          a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp, a.dbg_forces, a.ntiles,
                                          ctr(a, 2));

@@ -28,7 +28,7 @@ struct StepArgs {
     uint32_t block;            // threads per block = particles per tile
     uint32_t grid_nbr;         // blocks of the neighbour passes (ntiles, or the persistent grid)
     uint32_t *tile_ctr;        // 4 tile counters for persistent neighbour passes, or nullptr
-    uint32_t variant;          // SPH_VARIANT_* bits: per-row walks, neighbour prefetch
+    uint32_t variant;          // SPH_VARIANT_* bits: per-row walks, force register budget
     uint32_t any_tension;      // nonzero when some live scene has surface tension on
     uint32_t *dbg_nbr;         // optional: neighbour counts per sorted slot
     float4 *dbg_forces;        // optional: 4 force vectors per sorted slot

@@ -35,7 +35,7 @@ def test_configs_bit_identical(exe):
 
 @pytest.mark.parametrize("variant", [1, 2, 4, 7])
 def test_variants_bit_identical(variant):
-    """Per-row density/XSPH walks and the prefetching force kernel visit
+    """Per-row density/XSPH walks and the 64-register force kernel visit
     neighbours in the same order as the default walks: identical results,
     with and without surface tension in the batch."""
     specs = W.batch_manifest(num_scenes=3, seed=37, nmin=2000, nmax=9000)
