@@ -39,6 +39,7 @@ class SphExec(C.Structure):
 VARIANT_DENSITY_ROWS = 0x1
 VARIANT_XSPH_ROWS = 0x2
 VARIANT_FORCE_OCC = 0x4
+VARIANT_FORCE_TABLE = 0x8
 
 
 class SphError(RuntimeError):

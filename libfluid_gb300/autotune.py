@@ -5,7 +5,8 @@ choice computes bit-identical values; tests/test_exec_configs_gpu.py checks
 it): particles per tile (= threads per block), persistent blocks per SM for
 the neighbour passes (0 = one block per tile), the neighbour-mask skin, and
 then, on the best of those, the kernel-variant bits (per-row density and XSPH
-walks, the force kernel's register budget).  Each candidate is timed with CUDA
+walks, the force kernel's register budget and row-table walk).  Each
+candidate is timed with CUDA
 events over graph-replayed substeps after warm-up.  The best configuration
 per workload is written to tuned.json next to this file; the engine's
 compiled-in defaults (ExecConfig in csrc/engine.h) follow that record.
@@ -26,7 +27,7 @@ TUNED = os.path.join(HERE, "tuned.json")
 TILES = (128, 256)
 PERSISTENT = (0, 2, 4)
 SKINS = (0.1, 0.15, 0.2, 0.3)
-VARIANTS = tuple(range(8))
+VARIANTS = tuple(range(16))
 
 
 def load(workload: str) -> dict | None:

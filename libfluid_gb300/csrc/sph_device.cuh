@@ -195,6 +195,61 @@ struct MaskWalk {
     }
 };
 
+// Row table of one particle's neighbourhood, kept in the block's shared
+// memory (a column per thread: entry e of thread t at tab[e*ts + t]):
+// entries 0-8 the first slot jb of each row, 9-17 the row's mask word (or,
+// for a row longer than 32 candidates, its length).  `live` has a bit per
+// row with something to visit, `full` per row walked in full.  All 27 loads
+// are independent, so they are issued together, and TableWalk below moves
+// between rows with two shared-memory reads instead of dependent global loads.
+__device__ __forceinline__ void build_row_table(const DevParams& P, const uint32_t* __restrict__ start,
+                                                uint32_t cell_base, uint32_t delta, int3 g,
+                                                const uint32_t* __restrict__ mask, size_t stride, uint32_t k,
+                                                uint32_t* tab, uint32_t ts, uint32_t& live, uint32_t& full) {
+    live = 0u;
+    full = 0u;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        uint32_t jb, je;
+        const uint32_t w = __ldg(mask + (size_t)r * stride + k);
+        if (!row_range(P, start, cell_base, delta, g, r, jb, je)) continue;
+        const uint32_t len = je - jb;
+        const bool f = len > 32u;
+        const uint32_t v = f ? len : w;
+        if (f) full |= 1u << r;
+        if (v) live |= 1u << r;
+        tab[r * ts] = jb;
+        tab[(9 + r) * ts] = v;
+    }
+}
+
+// Walk of a row table in MaskWalk's order (rows ascending, candidates of a row
+// ascending).
+struct TableWalk {
+    const uint32_t* tab;
+    uint32_t ts, live, full, jb, bits, j, je;
+    __device__ __forceinline__ TableWalk(const uint32_t* tab_, uint32_t ts_, uint32_t live_, uint32_t full_)
+        : tab(tab_), ts(ts_), live(live_), full(full_), jb(0), bits(0), j(0), je(0) {}
+    __device__ __forceinline__ bool next(uint32_t& cand) {
+        for (;;) {
+            if (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                cand = jb + (uint32_t)b;
+                return true;
+            }
+            if (j < je) { cand = j++; return true; }
+            if (!live) return false;
+            const int r = __ffs(live) - 1;
+            live &= live - 1u;
+            jb = tab[r * ts];
+            const uint32_t w = tab[(9 + r) * ts];
+            if ((full >> r) & 1u) { j = jb; je = jb + w; }
+            else bits = w;
+        }
+    }
+};
+
 // Walk of every candidate of the 27 cells, flattened across the 9 rows.
 struct RangeWalk {
     const DevParams& P;

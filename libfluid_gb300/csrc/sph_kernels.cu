@@ -213,12 +213,13 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 }
 
 // ---------------------------------------------------------------------------
-// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84).  ROWS selects
-// one candidate loop per (y,z) row with two loads in flight (true) or one
-// loop flattened across the rows (false); the candidates and their order are
-// the same.
+// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84).  WALK selects
+// one loop flattened across the rows (0) or one candidate loop per (y,z) row
+// with two loads in flight (1); the candidates and their order are the same.
+// (A flattened loop over a row table in shared memory measured slower here:
+// 64 registers against 48.)
 // ---------------------------------------------------------------------------
-template <bool ROWS>
+template <int WALK>
 __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restrict__ params,
                                                       const DevScene* __restrict__ scenes,
                                                       const uint4* __restrict__ tiles,
@@ -264,7 +265,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
             }
         }
     };
-    if (ROWS) {
+    if (WALK == 1) {
 #pragma unroll 1
         for (int rr = 0; rr < 9; ++rr) {
             uint32_t jb0, je0, bs0 = 0u, be0 = 0u;
@@ -380,7 +381,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
 // budget as resident blocks of 256 threads per SM: 3 (85 registers; the
 // tension-free build needs 72, the tension build 80, no spills) or 4 (64
 // registers, more warps per SM, a few spilled values).
-template <bool TENSION, int MINB>
+template <bool TENSION, int MINB, bool TABLE>
 __global__ void __launch_bounds__(SPH_TILE, MINB)
 k_force_integrate(const DevParams* __restrict__ params,
                                                               const DevScene* __restrict__ scenes,
@@ -418,53 +419,65 @@ k_force_integrate(const DevParams* __restrict__ params,
         float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
         if (tension) ni = N[k];
         const float h2 = pp.h2, eps = pp.eps, inv_ri2 = si.w;
-        // exact neighbours recorded by the density pass (mask words 9-17)
-        MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
         // 2 rho0 / (rho_i + rho_i) of the tension sum (fluidphysics.cu:293), once per particle
         const float tden = (2.0f * pp.rest_density) / (ri + ri);
         const float sm = -pp.surface_tension * pp.mass;
         const float coh_m = -pp.mass * pp.mass;
-        uint32_t j;
-        while (walk.next(j)) {
-            // The mask holds exact neighbours, so position, (rho, p, c^2, 1/rho^2)
-            // and velocity of nearly every j are needed: the loads are issued
-            // together, before any test, so their latencies overlap.
-            const float4 pj = __ldg(P1 + j), sj = __ldg(S + j), vj = __ldg(V1 + j);
-            float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (tension) nj = __ldg(N + j);
-            const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
-            const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-            if (r2 <= h2 && r2 > eps && j != k && sj.x > eps) {
-                // r is the correctly rounded root: h - r below cancels, and pairs at
-                // r ~ h must see the reference's r; 1/r only scales (approximate)
-                const float r = sqrtf(r2);
-                const float inv_r = rsqrtf(r2);
-                const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
-                // artificial viscosity -visc (cs_i + cs_j) mu / (rho_i + rho_j),
-                // mu = h ux / (r^2 + 0.01 h^2), only for approaching pairs;
-                // evaluated without a branch (finite for every pair) and selected
-                const float Pv = __fdividef(-pp.viscosity * (csi + sj.z) * (pp.h * ux),
-                                            (r2 + pp.visc_eps) * (ri + sj.x));
-                const float Pi = (ux < 0.0f) ? Pv : 0.0f;
-                // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
-                const float mid = sj.y * inv_ri2 + pri * sj.w;
-                const float sr = (pp.mass * grad_spiky(pp, r)) * inv_r;
-                const float cx = sr * rx, cy = sr * ry, cz = sr * rz;
-                fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
-                const float mp = mid + Pi;
-                fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
-                if (tension) {
-                    // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
-                    // sigma == 0 the tension force is sigma * (finite sum) = 0, so
-                    // the term is skipped.
-                    const float sc2 = coh_m * cohesion_k(pp, r) * inv_r;
-                    const float hx = sc2 * rx, hy = sc2 * ry, hz = sc2 * rz;
-                    const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
-                    ftx = fmaf(tden, hx + kx, ftx);
-                    fty = fmaf(tden, hy + ky, fty);
-                    ftz = fmaf(tden, hz + kz, ftz);
+        auto run = [&](auto& walk) {
+            uint32_t j;
+            while (walk.next(j)) {
+                // The mask holds exact neighbours, so position, (rho, p, c^2, 1/rho^2)
+                // and velocity of nearly every j are needed: the loads are issued
+                // together, before any test, so their latencies overlap.
+                const float4 pj = __ldg(P1 + j), sj = __ldg(S + j), vj = __ldg(V1 + j);
+                float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (tension) nj = __ldg(N + j);
+                const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
+                const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+                if (r2 <= h2 && r2 > eps && j != k && sj.x > eps) {
+                    // r is the correctly rounded root: h - r below cancels, and pairs at
+                    // r ~ h must see the reference's r; 1/r only scales (approximate)
+                    const float r = sqrtf(r2);
+                    const float inv_r = rsqrtf(r2);
+                    const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
+                    // artificial viscosity -visc (cs_i + cs_j) mu / (rho_i + rho_j),
+                    // mu = h ux / (r^2 + 0.01 h^2), only for approaching pairs;
+                    // evaluated without a branch (finite for every pair) and selected
+                    const float Pv = __fdividef(-pp.viscosity * (csi + sj.z) * (pp.h * ux),
+                                                (r2 + pp.visc_eps) * (ri + sj.x));
+                    const float Pi = (ux < 0.0f) ? Pv : 0.0f;
+                    // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
+                    const float mid = sj.y * inv_ri2 + pri * sj.w;
+                    const float sr = (pp.mass * grad_spiky(pp, r)) * inv_r;
+                    const float cx = sr * rx, cy = sr * ry, cz = sr * rz;
+                    fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
+                    const float mp = mid + Pi;
+                    fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
+                    if (tension) {
+                        // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
+                        // sigma == 0 the tension force is sigma * (finite sum) = 0, so
+                        // the term is skipped.
+                        const float sc2 = coh_m * cohesion_k(pp, r) * inv_r;
+                        const float hx = sc2 * rx, hy = sc2 * ry, hz = sc2 * rz;
+                        const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
+                        ftx = fmaf(tden, hx + kx, ftx);
+                        fty = fmaf(tden, hy + ky, fty);
+                        ftz = fmaf(tden, hz + kz, ftz);
+                    }
                 }
             }
+        };
+        // exact neighbours recorded by the density pass (mask words 9-17)
+        if constexpr (TABLE) {
+            extern __shared__ uint32_t s_rows[];
+            uint32_t live, full;
+            build_row_table(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k,
+                            s_rows + threadIdx.x, blockDim.x, live, full);
+            TableWalk walk(s_rows + threadIdx.x, blockDim.x, live, full);
+            run(walk);
+        } else {
+            MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
+            run(walk);
         }
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
         ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
@@ -551,11 +564,12 @@ __device__ __forceinline__ void xsph_pair(const float4* __restrict__ P0, const f
 // reference updates velocities in place while neighbours read them (a race);
 // here reads see V2 and the result goes to V0 (Jacobi).
 // ---------------------------------------------------------------------------
-// ROWS selects the candidate walk: one loop per (y,z) row (true) or one loop
-// flattened across the rows (false); both visit the same candidates in the
-// same order.
+// WALK selects the candidate walk: 0 one loop flattened across the rows, 1 one
+// loop per (y,z) row; both visit the same candidates in the same order.  (The
+// row-table walk of the force pass measured slower here, 72 registers against
+// 54: the pair term is too light to pay for the table.)
 // (no __launch_bounds__: with it ptxas caps this kernel at 48 registers and spills)
-template <bool ROWS>
+template <int WALK>
 __global__ void k_xsph(const DevParams* __restrict__ params,
                                                    const DevScene* __restrict__ scenes,
                                                    const uint4* __restrict__ tiles,
@@ -587,7 +601,7 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
     // moved less than skin*h/2 each, which the force pass recorded.
     uint32_t j;
     const bool masked = __uint_as_float(__ldg(maxdisp)) <= pp.xsph_disp_limit2;
-    if (ROWS) {
+    if (WALK == 1) {
         auto visit = [&](uint32_t jj) { xsph_pair(P0, V2, jj, k, pi, vi, h2, h, c6, two_m, eps, sx, sy, sz); };
         if (masked) for_masked(pp, start, sc.cell_base, delta, g, mask, mask_stride, k, visit);   // skin words 0-8
         else for_candidates(pp, start, sc.cell_base, delta, g, visit);
@@ -712,7 +726,7 @@ cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
-    auto kern = (a.variant & SPH_VARIANT_DENSITY_ROWS) ? k_density<true> : k_density<false>;
+    auto kern = (a.variant & SPH_VARIANT_DENSITY_ROWS) ? k_density<1> : k_density<0>;
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
                                          a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
@@ -724,15 +738,20 @@ cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
 }
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
     const bool occ = (a.variant & SPH_VARIANT_FORCE_OCC) != 0u;
-    auto kern = a.any_tension ? (occ ? k_force_integrate<true, 4> : k_force_integrate<true, 3>)
-                              : (occ ? k_force_integrate<false, 4> : k_force_integrate<false, 3>);
-    kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S, a.N, a.mask,
+    const bool table = (a.variant & SPH_VARIANT_FORCE_TABLE) != 0u;
+    auto kern = a.any_tension
+                    ? (table ? (occ ? k_force_integrate<true, 4, true> : k_force_integrate<true, 3, true>)
+                             : (occ ? k_force_integrate<true, 4, false> : k_force_integrate<true, 3, false>))
+                    : (table ? (occ ? k_force_integrate<false, 4, true> : k_force_integrate<false, 3, true>)
+                             : (occ ? k_force_integrate<false, 4, false> : k_force_integrate<false, 3, false>));
+    const size_t smem = table ? (size_t)18 * a.block * sizeof(uint32_t) : 0;
+    kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S, a.N, a.mask,
                                          a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp, a.dbg_forces, a.ntiles,
                                          ctr(a, 2));
     return cudaGetLastError();
 }
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st) {
-    auto kern = (a.variant & SPH_VARIANT_XSPH_ROWS) ? k_xsph<true> : k_xsph<false>;
+    auto kern = (a.variant & SPH_VARIANT_XSPH_ROWS) ? k_xsph<1> : k_xsph<0>;
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.mask,
                                          a.mask_stride, a.maxdisp, a.V0, a.ntiles, ctr(a, 3));
     return cudaGetLastError();

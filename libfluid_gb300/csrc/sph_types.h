@@ -50,8 +50,9 @@ struct DevParams {
 #define SPH_VARIANT_DENSITY_ROWS  0x1u   // density: one loop per cell row, two loads in flight
 #define SPH_VARIANT_XSPH_ROWS     0x2u   // XSPH: one loop per cell row instead of one flattened walk
 #define SPH_VARIANT_FORCE_OCC     0x4u   // force: 64-register build (more resident warps)
-#define SPH_VARIANT_MASK          0x7u
-#define SPH_VARIANT_DEFAULT       0x7u   // measured fastest on the 1M dam break and the 256-scene batch
+#define SPH_VARIANT_FORCE_TABLE   0x8u   // force: walk over a per-thread row table in shared memory
+#define SPH_VARIANT_MASK          0xfu
+#define SPH_VARIANT_DEFAULT       0xfu   // measured fastest on the 1M dam break and the 256-scene batch
 
 // Scene placement in the engine's arenas.
 struct DevScene {

@@ -33,11 +33,11 @@ def test_configs_bit_identical(exe):
         assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4, 7])
+@pytest.mark.parametrize("variant", [1, 2, 4, 7, 8, 12, 15])
 def test_variants_bit_identical(variant):
-    """Per-row density/XSPH walks and the 64-register force kernel visit
-    neighbours in the same order as the default walks: identical results,
-    with and without surface tension in the batch."""
+    """Per-row density/XSPH walks, the 64-register force kernel and the
+    force kernel's row-table walk visit neighbours in the same order as the
+    default walks: identical results, with and without surface tension."""
     specs = W.batch_manifest(num_scenes=3, seed=37, nmin=2000, nmax=9000)
     specs.append(W.small_dam_break(seed=10))
     base = _run(specs, 6, tile=128, persistent=0, skin=0.1, variant=0)
