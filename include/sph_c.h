@@ -191,12 +191,13 @@ int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
  * blocks per SM taking tiles from a counter in the neighbour passes; skin:
  * neighbour-mask skin in units of h, in (0, 1]; variant: SPH_VARIANT_* bits
  * choosing how the neighbour walks are scheduled.  Defaults: tile 128,
- * persistent 0, skin 0.1, variant 15 (per-row density and XSPH walks,
- * 64-register force build walking a row table). */
+ * persistent 0, skin 0.1, variant 31 (per-row density and XSPH walks,
+ * 64-register force build; force and normal passes walk a row table). */
 #define SPH_VARIANT_DENSITY_ROWS   0x1u  /* density: one loop per cell row */
 #define SPH_VARIANT_XSPH_ROWS      0x2u  /* XSPH: one loop per cell row */
 #define SPH_VARIANT_FORCE_OCC      0x4u  /* force: 64-register build, more resident warps */
 #define SPH_VARIANT_FORCE_TABLE    0x8u  /* force: row table in shared memory */
+#define SPH_VARIANT_NORMALS_TABLE  0x10u /* normals: row table in shared memory */
 typedef struct sph_exec_config {
     uint32_t tile;
     uint32_t persistent;

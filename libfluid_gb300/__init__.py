@@ -201,7 +201,7 @@ class FluidSystem:
     def setUseGraph(self, on: bool) -> None:
         self._ck(self._L.sph_set_use_graph(self._h, 1 if on else 0))
 
-    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 15) -> None:
+    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 31) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_set_exec(self._h, C.byref(e)))

@@ -40,6 +40,7 @@ VARIANT_DENSITY_ROWS = 0x1
 VARIANT_XSPH_ROWS = 0x2
 VARIANT_FORCE_OCC = 0x4
 VARIANT_FORCE_TABLE = 0x8
+VARIANT_NORMALS_TABLE = 0x10
 
 
 class SphError(RuntimeError):

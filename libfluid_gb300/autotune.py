@@ -5,13 +5,14 @@ choice computes bit-identical values; tests/test_exec_configs_gpu.py checks
 it): particles per tile (= threads per block), persistent blocks per SM for
 the neighbour passes (0 = one block per tile), the neighbour-mask skin, and
 then, on the best of those, the kernel-variant bits (per-row density and XSPH
-walks, the force kernel's register budget and row-table walk).  Each
-candidate is timed with CUDA
-events over graph-replayed substeps after warm-up.  The best configuration
-per workload is written to tuned.json next to this file; the engine's
-compiled-in defaults (ExecConfig in csrc/engine.h) follow that record.
+walks, the force kernel's register budget, row-table walks of the force and
+normal passes).  Each candidate is timed with CUDA events over graph-replayed
+substeps after warm-up.  The best configuration per workload is written to
+tuned.json next to this file; the engine's compiled-in defaults (ExecConfig
+in csrc/engine.h) follow that record.
 
-    python -m libfluid_gb300.autotune [--workload batched|dam_break_1m|all] [--steps 20]
+    python -m libfluid_gb300.autotune [--workload batched|dam_break_1m|large_tension|all]
+                                      [--steps 20] [--variants-only]
 """
 from __future__ import annotations
 
@@ -27,7 +28,7 @@ TUNED = os.path.join(HERE, "tuned.json")
 TILES = (128, 256)
 PERSISTENT = (0, 2, 4)
 SKINS = (0.1, 0.15, 0.2, 0.3)
-VARIANTS = tuple(range(16))
+VARIANTS = tuple(range(32))
 
 
 def load(workload: str) -> dict | None:
@@ -45,6 +46,8 @@ def _scenes(workload: str):
         return [W.dam_break_1m()]
     if workload == "small_dam_break":
         return [W.small_dam_break()]
+    if workload == "large_tension":
+        return [W.large_tension()]
     raise ValueError(workload)
 
 
@@ -68,11 +71,12 @@ def time_config(scenes, tile: int, persistent: int, skin: float, steps: int, war
     return ms
 
 
-def tune(workload: str, steps: int = 20, device: int = 0) -> dict:
+def tune(workload: str, steps: int = 20, device: int = 0, variants_only: bool = False) -> dict:
     scenes = _scenes(workload)
     n = sum(s.n for s in scenes)
     trials = []
-    for tile, pers, skin in itertools.product(TILES, PERSISTENT, SKINS):
+    grid = [(128, 0, 0.1)] if variants_only else itertools.product(TILES, PERSISTENT, SKINS)
+    for tile, pers, skin in grid:
         ms = time_config(scenes, tile, pers, skin, steps, device=device)
         trials.append({"tile": tile, "persistent": pers, "skin": skin, "variant": 0, "ms_per_step": ms,
                        "particle_steps_per_s": n / (ms * 1e-3)})
@@ -92,6 +96,8 @@ def main():
     ap.add_argument("--workload", default="all")
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--out", default=TUNED)
+    ap.add_argument("--variants-only", action="store_true",
+                    help="keep tile 128, persistent 0, skin 0.1 and sweep the kernel variants only")
     args = ap.parse_args()
     names = ["dam_break_1m", "batched", "small_dam_break"] if args.workload == "all" else [args.workload]
     try:
@@ -99,7 +105,7 @@ def main():
     except (OSError, ValueError):
         tuned = {}
     for w in names:
-        r = tune(w, args.steps)
+        r = tune(w, args.steps, variants_only=args.variants_only)
         tuned[w] = r
         print(w, r["best"], "%.4f ms/step" % min(t["ms_per_step"] for t in r["trials"]), flush=True)
     with open(args.out, "w") as f:

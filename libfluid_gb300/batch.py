@@ -70,7 +70,11 @@ class Batch:
         p = params_struct(spec)
         self._ck(self._L.sph_batch_add_scene(self._h, C.byref(p), spec.n, C.byref(sid)))
         self.scenes[sid.value] = spec
-        if generate:
+        if generate and getattr(spec, "extra_pos", None) is not None:
+            # particles beyond the lattice blocks come from the host (the
+            # lattice part is identical to the device generator's)
+            self.set_state(sid.value, spec.positions(), spec.velocities())
+        elif generate:
             first = 0
             for b in spec.blocks:
                 s = lattice_struct(b)
@@ -142,7 +146,7 @@ class Batch:
     def set_use_graph(self, on: bool) -> None:
         self._ck(self._L.sph_batch_set_use_graph(self._h, 1 if on else 0))
 
-    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 15) -> None:
+    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 31) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_batch_set_exec(self._h, C.byref(e)))

@@ -319,8 +319,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
 // ---------------------------------------------------------------------------
 // Surface normals (computeNormals, fluidphysics.cu:154-210).  Only launched
 // for scenes with surface tension: with sigma == 0 the normals enter the
-// force only through sigma * (...), which is exactly zero.
+// force only through sigma * (...), which is exactly zero.  TABLE walks a row
+// table in shared memory as the force pass does; same neighbours, same order.
 // ---------------------------------------------------------------------------
+template <bool TABLE>
 __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restrict__ params,
                                                       const DevScene* __restrict__ scenes,
                                                       const uint4* __restrict__ tiles,
@@ -344,25 +346,38 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
-    uint32_t j;
     // m gradPoly6(r) rvec / (rho_j r) = m c (h^2 - r^2)^2 rvec / rho_j: the
     // factor r of gradPoly6 cancels the 1/r; h^2 - r^2 is formed from the
     // rounded root r as gradPoly6 forms it (it cancels near r = h)
     const float mc = pp.mass * pp.grad_poly6;
-    while (walk.next(j)) {
-        const float4 q = __ldg(P1 + j);
-        const float rhoj = __ldg(&S[j].x);
-        const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
-        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (r2 <= pp.h2 && r2 > pp.eps && j != k && rhoj > pp.eps) {
-            const float r = sqrtf(r2);
-            const float x = fmaf(-r, r, pp.h2);
-            const float s = (r >= pp.h) ? 0.0f : __fdividef(mc * (x * x), rhoj);
-            sx = fmaf(s, rx, sx);
-            sy = fmaf(s, ry, sy);
-            sz = fmaf(s, rz, sz);
+    auto run = [&](auto& walk) {
+        uint32_t j;
+        while (walk.next(j)) {
+            const float4 q = __ldg(P1 + j);
+            const float rhoj = __ldg(&S[j].x);
+            const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
+            const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+            if (r2 <= pp.h2 && r2 > pp.eps && j != k && rhoj > pp.eps) {
+                const float r = sqrtf(r2);
+                const float x = fmaf(-r, r, pp.h2);
+                const float s = (r >= pp.h) ? 0.0f : __fdividef(mc * (x * x), rhoj);
+                sx = fmaf(s, rx, sx);
+                sy = fmaf(s, ry, sy);
+                sz = fmaf(s, rz, sz);
+            }
         }
+    };
+    // exact neighbours recorded by the density pass (mask words 9-17)
+    if constexpr (TABLE) {
+        extern __shared__ uint32_t s_rows[];
+        uint32_t live, full;
+        build_row_table(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k,
+                        s_rows + threadIdx.x, blockDim.x, live, full);
+        TableWalk walk(s_rows + threadIdx.x, blockDim.x, live, full);
+        run(walk);
+    } else {
+        MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
+        run(walk);
     }
     N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
   });
@@ -732,8 +747,11 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
-    k_normals<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask,
-                                              a.mask_stride, a.N, a.ntiles, ctr(a, 1));
+    const bool table = (a.variant & SPH_VARIANT_NORMALS_TABLE) != 0u;
+    auto kern = table ? k_normals<true> : k_normals<false>;
+    const size_t smem = table ? (size_t)18 * a.block * sizeof(uint32_t) : 0;
+    kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
+                                            a.N, a.ntiles, ctr(a, 1));
     return cudaGetLastError();
 }
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {

@@ -51,8 +51,10 @@ struct DevParams {
 #define SPH_VARIANT_XSPH_ROWS     0x2u   // XSPH: one loop per cell row instead of one flattened walk
 #define SPH_VARIANT_FORCE_OCC     0x4u   // force: 64-register build (more resident warps)
 #define SPH_VARIANT_FORCE_TABLE   0x8u   // force: walk over a per-thread row table in shared memory
-#define SPH_VARIANT_MASK          0xfu
-#define SPH_VARIANT_DEFAULT       0xfu   // measured fastest on the 1M dam break and the 256-scene batch
+#define SPH_VARIANT_NORMALS_TABLE 0x10u  // normals: the same
+#define SPH_VARIANT_MASK          0x1fu
+#define SPH_VARIANT_DEFAULT       0x1fu  // measured fastest on the 1M dam break, the 256-scene batch
+                                         // and the 8M tension scene
 
 // Scene placement in the engine's arenas.
 struct DevScene {

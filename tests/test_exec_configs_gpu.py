@@ -33,7 +33,7 @@ def test_configs_bit_identical(exe):
         assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4, 7, 8, 12, 15])
+@pytest.mark.parametrize("variant", [1, 2, 4, 7, 8, 12, 15, 16, 31])
 def test_variants_bit_identical(variant):
     """Per-row density/XSPH walks, the 64-register force kernel and the
     force kernel's row-table walk visit neighbours in the same order as the
