@@ -110,6 +110,7 @@ Engine::Engine(int device) {
     cudaMalloc((void**)&scal_, 8 * sizeof(uint32_t));
     cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_);
     for (auto& e : ev_) cudaEventCreate(&e);
+    init_kernel_attributes();   // a performance hint only: launches work without it
 }
 
 Engine::~Engine() {

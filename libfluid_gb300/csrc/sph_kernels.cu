@@ -716,6 +716,24 @@ cudaError_t launch_hash(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 static inline uint32_t* ctr(const StepArgs& a, int k) { return a.tile_ctr ? a.tile_ctr + k : nullptr; }
+
+// Kernels with a row table in shared memory need 72 B per thread of it; left
+// to itself the driver may give them the largest shared-memory carveout and
+// shrink L1, which holds the neighbour gathers.  Ask for the smallest carveout
+// that still fits 8 blocks of 128 threads (8 x 9 KB + per-block reserve).
+cudaError_t init_kernel_attributes() {
+    const int pct = SPH_TABLE_CARVEOUT_PCT;
+    const void* fns[] = {
+        (const void*)k_force_integrate<true, 3, true>, (const void*)k_force_integrate<true, 4, true>,
+        (const void*)k_force_integrate<false, 3, true>, (const void*)k_force_integrate<false, 4, true>,
+        (const void*)k_normals<true>};
+    for (const void* f : fns) {
+        const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
     const uint32_t n = a.total_cells;
     const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;

@@ -34,6 +34,14 @@ struct StepArgs {
     float4 *dbg_forces;        // optional: 4 force vectors per sorted slot
 };
 
+// Shared-memory carveout (percent of the SM's maximum) requested for the
+// kernels that keep a row table in shared memory.
+#ifndef SPH_TABLE_CARVEOUT_PCT
+#define SPH_TABLE_CARVEOUT_PCT 40
+#endif
+// One-time per-device kernel attributes (call before the first launch).
+cudaError_t init_kernel_attributes();
+
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st);
 // Exclusive scan of counts[0,n) into starts[0,n] with caller-provided tile
