@@ -154,6 +154,24 @@ def profile_traffic(kernel: str, workload: str):
     return None
 
 
+def profile_counters(kernel: str, workload: str):
+    """Issue-side ncu counters of a kernel from the committed summary, or None:
+    the neighbour passes are bound by instruction issue and gather latency,
+    which the HBM fraction alone does not show."""
+    path = os.path.join(ROOT, "profiles", f"counters_{workload}.txt")
+    keys = ("issue_active_pct", "lanes_per_inst", "fma_pipe_pct", "alu_pipe_pct", "dram_pct")
+    try:
+        for line in open(path):
+            p = line.split()
+            if len(p) == 1 + len(keys) and p[0] == kernel:
+                d = {k: float(v) for k, v in zip(keys, p[1:])}
+                d["source"] = f"profiles/counters_{workload}.txt (ncu --set full)"
+                return d
+    except OSError:
+        pass
+    return None
+
+
 def configure(fs, spec, pos, vel):
     fs.init(spec.n, spec.unit_cube_res or 1)
     if not spec.unit_cube_res:
@@ -326,7 +344,8 @@ def run_ours(args, dist):
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback 6.8 TB/s",
                 "step_alg_bytes": sum(ALG_BYTES[k] for k in ("hash", "sort", "density", "force_integrate", "xsph"))
                 * n + CELL_BYTES * cells,
-                "pass_share": {k: v / per_launch["substep"] for k, v in kern.items()}}
+                "pass_share": {k: v / per_launch["substep"] for k, v in kern.items()},
+                "issue": profile_counters(dom, args.workload)}
     roofline["step_frac"] = roofline["step_alg_bytes"] / (ms_max / args.steps * 1e-3) / 1e9 / peak
 
     # ---- end to end through the C ABI with pinned host buffers ----
