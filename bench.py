@@ -564,8 +564,10 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-refcuda", action="store_true")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
-    ap.add_argument("--requests", type=int, default=1000, help="served workload: number of requests")
-    ap.add_argument("--rates", type=float, nargs="+", default=[50, 200, 500, 1000, 2000],
+    ap.add_argument("--requests", type=int, default=400, help="served workload: number of requests")
+    # the knee is near 55 req/s (mean request 1.25e7 particle-steps, ~7e8 particle-steps/s
+    # served): two rates below it show unloaded latency, the rest saturation
+    ap.add_argument("--rates", type=float, nargs="+", default=[10, 25, 50, 200, 1000],
                     help="served workload: Poisson arrival rates (req/s)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup

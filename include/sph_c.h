@@ -205,6 +205,16 @@ typedef struct sph_exec_config {
     uint32_t variant;
 } sph_exec_config;
 int sph_set_exec(sph_system* s, const sph_exec_config* e);
+/* XSPH schedule (no counterpart: the reference ends every substep with its
+ * XSPH pass).  on != 0, the default: a substep ends after the integrator and
+ * its XSPH update is applied by the next substep's density pass, in the same
+ * neighbour walk; reading a system's state (export, snapshot) computes the
+ * update on demand without changing the run.  The pairs are exactly the
+ * reference's (its previous cell lists are honoured); only the summation
+ * order of the XSPH sums differs from the per-substep schedule (on == 0).
+ * Debug taps imply the per-substep schedule, as do grids of more than 1024
+ * cells along an axis. */
+int sph_set_deferred_xsph(sph_system* s, int on);
 int sph_get_exec(const sph_system* s, sph_exec_config* e);
 int sph_set_use_graph(sph_system* s, int on);     /* CUDA-graph replay of the substep (default on) */
 int sph_set_profiling(sph_system* s, int on);     /* per-pass CUDA events (disables the graph) */
@@ -265,6 +275,7 @@ int sph_batch_debug_enable(sph_batch* b, int on);
 int sph_batch_debug_get(sph_batch* b, int scene_id, int field, void* buf, uint64_t count);
 int sph_batch_set_use_graph(sph_batch* b, int on);
 int sph_batch_set_exec(sph_batch* b, const sph_exec_config* e);
+int sph_batch_set_deferred_xsph(sph_batch* b, int on);
 int sph_batch_timer_mark(sph_batch* b, int slot);
 int sph_batch_timer_elapsed(sph_batch* b, int a, int b2, float* ms);
 const char* sph_batch_last_error(const sph_batch* b);

@@ -206,6 +206,11 @@ class FluidSystem:
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_set_exec(self._h, C.byref(e)))
 
+    def setDeferredXSPH(self, on: bool) -> None:
+        """XSPH applied by the next substep's density pass (default) or at the
+        end of every substep, as the reference does."""
+        self._ck(self._L.sph_set_deferred_xsph(self._h, 1 if on else 0))
+
     def getExec(self) -> dict:
         from ._capi import SphExec
         e = SphExec()

@@ -100,6 +100,7 @@ SIGNATURES = [
     ("sph_set_use_graph", _I, [_P, _I]),
     ("sph_set_profiling", _I, [_P, _I]),
     ("sph_set_exec", _I, [_P, C.POINTER(SphExec)]),
+    ("sph_set_deferred_xsph", _I, [_P, _I]),
     ("sph_get_exec", _I, [_P, C.POINTER(SphExec)]),
     ("sph_get_pass_times", _I, [_P, C.POINTER(C.c_double), _I, C.POINTER(C.c_uint64)]),
     ("sph_pass_name", C.c_char_p, [_I]),

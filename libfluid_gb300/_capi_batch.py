@@ -32,6 +32,7 @@ SIGNATURES = [
     ("sph_batch_debug_get", _I, [_P, _I, _I, _P, C.c_uint64]),
     ("sph_batch_set_use_graph", _I, [_P, _I]),
     ("sph_batch_set_exec", _I, [_P, _P]),
+    ("sph_batch_set_deferred_xsph", _I, [_P, _I]),
     ("sph_batch_timer_mark", _I, [_P, _I]),
     ("sph_batch_timer_elapsed", _I, [_P, _I, _I, C.POINTER(_F)]),
     ("sph_batch_last_error", C.c_char_p, [_P]),

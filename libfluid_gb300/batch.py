@@ -86,6 +86,12 @@ class Batch:
         self._ck(self._L.sph_batch_remove_scene(self._h, sid))
         self.scenes.pop(sid, None)
 
+    def set_params(self, sid: int, spec: SceneSpec) -> None:
+        """Replace a scene's parameters with those of `spec` (state is kept)."""
+        p = params_struct(spec)
+        self._ck(self._L.sph_batch_set_params(self._h, sid, C.byref(p)))
+        self.scenes[sid] = spec
+
     def set_state(self, sid: int, pos, vel=None) -> None:
         p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
         v = None if vel is None else np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
@@ -150,6 +156,9 @@ class Batch:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_batch_set_exec(self._h, C.byref(e)))
+
+    def set_deferred_xsph(self, on: bool) -> None:
+        self._ck(self._L.sph_batch_set_deferred_xsph(self._h, 1 if on else 0))
 
     def timer_mark(self, slot: int) -> None:
         self._ck(self._L.sph_batch_timer_mark(self._h, slot))

@@ -404,6 +404,10 @@ int sph_set_use_graph(sph_system* s, int on) {
     s->eng->set_use_graph(on != 0);
     return SPH_OK;
 }
+int sph_set_deferred_xsph(sph_system* s, int on) {
+    if (!s) return SPH_EINVAL;
+    return eng_err(s, s->eng->set_deferred_xsph(on != 0));
+}
 int sph_set_exec(sph_system* s, const sph_exec_config* e) {
     if (!s || !e) return SPH_EINVAL;
     sph::ExecConfig x;

@@ -170,6 +170,10 @@ int sph_batch_set_use_graph(sph_batch* b, int on) {
     b->eng->set_use_graph(on != 0);
     return SPH_OK;
 }
+int sph_batch_set_deferred_xsph(sph_batch* b, int on) {
+    if (!b) return SPH_EINVAL;
+    return berr(b, b->eng->set_deferred_xsph(on != 0));
+}
 int sph_batch_set_exec(sph_batch* b, const sph_exec_config* e) {
     if (!b || !e) return SPH_EINVAL;
     sph::ExecConfig x;

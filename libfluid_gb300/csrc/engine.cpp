@@ -95,7 +95,7 @@ bool derive_params(const SceneConfig& c, DevParams& d, std::string* err) {
     return true;
 }
 
-uint64_t Engine::bytes_per_particle() { return 9 * 16 + 4 * 4 + 18 * 4; }
+uint64_t Engine::bytes_per_particle() { return 10 * 16 + 6 * 4 + 18 * 4; }
 uint64_t Engine::bytes_per_cell() { return 2 * 4 + 1; }
 const char* Engine::pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : "?"; }
 
@@ -117,8 +117,10 @@ Engine::~Engine() {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
     free_all();
-    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
-    if (graph_) cudaGraphDestroy(graph_);
+    if (exec_pre_) cudaGraphExecDestroy(exec_pre_);
+    if (exec_suf_) cudaGraphExecDestroy(exec_suf_);
+    if (graph_pre_) cudaGraphDestroy(graph_pre_);
+    if (graph_suf_) cudaGraphDestroy(graph_suf_);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     for (auto& e : timers_) if (e) cudaEventDestroy(e);
     if (status_) cudaFree(status_);
@@ -143,9 +145,10 @@ int Engine::cuda_fail(cudaError_t e, const char* what) {
     } while (0)
 
 void Engine::free_all() {
-    float4** f4[] = {&P0_, &P1_, &V0_, &V1_, &V2_, &A0_, &A1_, &S_, &N_, &dbg_forces_};
+    float4** f4[] = {&P0_, &P1_, &V0_, &V1_, &V2_, &A0_, &A1_, &S_, &N_, &Vc_, &dbg_forces_};
     for (auto p : f4) { if (*p) cudaFree(*p); *p = nullptr; }
-    uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &count_, &start_, &scan_sums_, &dbg_nbr_, &mask_};
+    uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &count_, &start_, &scan_sums_, &dbg_nbr_, &mask_,
+                      &okey_, &okey1_, &pend_};
     for (auto p : u) { if (*p) cudaFree(*p); *p = nullptr; }
     if (stage_) cudaFree(stage_);
     stage_ = nullptr;
@@ -169,8 +172,10 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
         uint64_t np = std::max<uint64_t>(parts, pcap_ + pcap_ / 2);
         if (byte_limit_ && np * bytes_per_particle() + std::max(cells, ccap_) * 8 > byte_limit_) np = parts;
         if (np >= (1ull << 31)) return fail(ENG_ENOMEM, "particle capacity exceeds 2^31");
-        float4** state[] = {&P0_, &V0_, &A0_, &S_};
-        float4** scratch[] = {&P1_, &V1_, &V2_, &A1_, &N_};
+        // state between substeps: P0, V0, A0, S, and for scenes with a
+        // pending XSPH update their post-integration velocities V2 and cells
+        float4** state[] = {&P0_, &V0_, &A0_, &S_, &V2_};
+        float4** scratch[] = {&P1_, &V1_, &A1_, &N_, &Vc_};
         for (auto p : state) {
             float4* q = nullptr;
             cudaError_t e = cudaMalloc((void**)&q, np * sizeof(float4));
@@ -182,13 +187,25 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
             }
             *p = q;
         }
+        {
+            uint32_t* q = nullptr;
+            cudaError_t e = cudaMalloc((void**)&q, np * sizeof(uint32_t));
+            if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+            if (okey_) {
+                ENG_CK(cudaMemcpyAsync(q, okey_, pcap_ * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream_), "grow copy");
+                ENG_CK(cudaStreamSynchronize(stream_), "grow sync");
+                cudaFree(okey_);
+            }
+            okey_ = q;
+        }
+        prefix_valid_ = false;
         for (auto p : scratch) {
             if (*p) cudaFree(*p);
             *p = nullptr;
             cudaError_t e = cudaMalloc((void**)p, np * sizeof(float4));
             if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
         }
-        uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_};
+        uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &okey1_};
         for (auto p : u) {
             if (*p) cudaFree(*p);
             *p = nullptr;
@@ -224,6 +241,7 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
             return fail(ENG_ENOMEM, "device allocation of cell arrays failed");
         ccap_ = nc;
         graph_dirty_ = true;
+        prefix_valid_ = false;
     }
     dev_bytes_ = pcap_ * bytes_per_particle() + ccap_ * 8;
     return ENG_OK;
@@ -324,6 +342,7 @@ int Engine::add_scene(const SceneConfig& cfg_in, uint32_t n, int* id_out) {
     if (rc) { free_slots(s.part_base, n); return rc; }
     scenes_.push_back(s);
     layout_dirty_ = params_dirty_ = true;
+    prefix_valid_ = false;
     if (id_out) *id_out = s.id;
     return ENG_OK;
 }
@@ -334,6 +353,7 @@ int Engine::remove_scene(int id) {
             free_slots(scenes_[k].part_base, scenes_[k].n);
             scenes_.erase(scenes_.begin() + k);
             layout_dirty_ = params_dirty_ = true;
+            prefix_valid_ = false;
             return ENG_OK;
         }
     }
@@ -348,6 +368,14 @@ int Engine::set_config(int id, const SceneConfig& cfg_in) {
         DevParams dp;
         std::string e;
         if (!derive_params(cfg, dp, &e)) return fail(ENG_EINVAL, e);
+        if (std::memcmp(&dp, &s.dp, sizeof(DevParams)) == 0 && dp.ncells == s.dp.ncells) {
+            s.cfg = cfg;
+            return ENG_OK;
+        }
+        // a pending XSPH update belongs to the substep that ran with the old
+        // parameters: apply it before they change
+        if (s.pending) { int rc = materialize(s); if (rc) return rc; }
+        prefix_valid_ = false;
         if (dp.ncells != s.dp.ncells || dp.flags != s.dp.flags) layout_dirty_ = true;
         s.cfg = cfg;
         if (std::memcmp(&dp, &s.dp, sizeof(DevParams)) != 0) params_dirty_ = true;
@@ -371,15 +399,20 @@ int Engine::rebuild_layout() {
     cell_base_.resize(ns);
     uint64_t cb = 0;
     any_tension_ = false;
+    std::vector<uint32_t> h_pend(ns);
     for (size_t k = 0; k < ns; ++k) {
-        const Scene& s = scenes_[k];
+        Scene& s = scenes_[k];
         cell_base_[k] = (uint32_t)cb;
         h_scenes_[k] = DevScene{s.part_base, s.n, (uint32_t)cb, s.dp.ncells};
         cb += s.dp.ncells + 1ull;
         const uint32_t tile = exec_.tile;
+        s.table_index = (uint32_t)k;
+        s.tile_first = (uint32_t)h_tiles_.size();
         for (uint32_t f = 0; f < s.n; f += tile)
             h_tiles_.push_back(make_uint4((uint32_t)k, s.part_base + f, std::min<uint32_t>(tile, s.n - f), 0u));
+        s.tile_count = (uint32_t)h_tiles_.size() - s.tile_first;
         any_tension_ = any_tension_ || (s.dp.flags & 1u);
+        h_pend[k] = s.pending ? 1u : 0u;
     }
     total_cells_ = (uint32_t)cb;
     int rc = ensure_capacity(slots_end_, cb);
@@ -394,6 +427,14 @@ int Engine::rebuild_layout() {
         ENG_CK(cudaMallocHost((void**)&h_params_, scene_cap_ * sizeof(DevParams)), "param staging");
         graph_dirty_ = true;
     }
+    if (ns > pend_cap_) {
+        if (pend_) cudaFree(pend_);
+        pend_cap_ = std::max<uint64_t>(ns, pend_cap_ * 2);
+        ENG_CK(cudaMalloc((void**)&pend_, pend_cap_ * sizeof(uint32_t)), "pending flags");
+        graph_dirty_ = true;
+    }
+    if (ns) ENG_CK(cudaMemcpyAsync(pend_, h_pend.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_),
+                   "pending flags upload");
     if (h_tiles_.size() > tile_cap_) {
         if (d_tiles_) cudaFree(d_tiles_);
         tile_cap_ = std::max<uint64_t>(h_tiles_.size(), tile_cap_ * 2);
@@ -414,7 +455,13 @@ int Engine::upload_params() {
     const size_t ns = scenes_.size();
     // The pinned staging buffer is reused: wait until the previous copy drained.
     ENG_CK(cudaStreamSynchronize(stream_), "param sync");
-    for (size_t k = 0; k < ns; ++k) h_params_[k] = scenes_[k].dp;
+    bool all_defer = true;
+    for (size_t k = 0; k < ns; ++k) {
+        h_params_[k] = scenes_[k].dp;
+        if (scene_defers(scenes_[k])) h_params_[k].flags |= SPH_FLAG_DEFER_XSPH;
+        else all_defer = false;
+    }
+    if (all_defer != all_defer_) { all_defer_ = all_defer; graph_dirty_ = true; }
     if (ns) ENG_CK(cudaMemcpyAsync(d_params_, h_params_, ns * sizeof(DevParams), cudaMemcpyHostToDevice, stream_), "param upload");
     params_dirty_ = false;
     return ENG_OK;
@@ -430,6 +477,7 @@ StepArgs Engine::args() const {
     a.P0 = P0_; a.V0 = V0_; a.A0 = A0_;
     a.P1 = P1_; a.V1 = V1_; a.A1 = A1_;
     a.V2 = V2_; a.S = S_; a.N = N_;
+    a.Vc = Vc_; a.okey = okey_; a.okey1 = okey1_; a.pend = pend_;
     a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
     a.key = key_; a.slot = slot_; a.tmp = tmp_; a.perm = perm_;
     a.status = status_;
@@ -446,8 +494,11 @@ StepArgs Engine::args() const {
     return a;
 }
 
-// Record (or launch) one substep on the stream.
-int Engine::launch_substep(bool profile) {
+// Record (or launch) the two halves of a substep on the stream.  The prefix
+// (sort and density, with any pending XSPH update) ends where a state read
+// needs it; the suffix is the rest (normals, forces and integrator, and the
+// XSPH pass of scenes that do not defer it).
+int Engine::launch_prefix(bool profile) {
     const StepArgs a = args();
     cudaStream_t st = stream_;
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
@@ -462,11 +513,18 @@ int Engine::launch_substep(bool profile) {
     mark(3);
     ENG_CK(launch_density(a, st), "density");
     mark(4);
+    return ENG_OK;
+}
+
+int Engine::launch_suffix(bool profile) {
+    const StepArgs a = args();
+    cudaStream_t st = stream_;
+    auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     if (any_tension_) ENG_CK(launch_normals(a, st), "normals");
     mark(5);
     ENG_CK(launch_force(a, st), "force");
     mark(6);
-    ENG_CK(launch_xsph(a, st), "xsph");
+    if (!all_defer_) ENG_CK(launch_xsph(a, st), "xsph");
     mark(7);
     return ENG_OK;
 }
@@ -484,36 +542,54 @@ int Engine::read_status() {
     return ENG_OK;
 }
 
-int Engine::step(uint32_t substeps, bool sync) {
-    cudaSetDevice(device_);
-    if (scenes_.empty()) return ENG_OK;
+// Layout, parameters and (in graph mode) the two captured graphs up to date.
+int Engine::prepare() {
     if (layout_dirty_) { int rc = rebuild_layout(); if (rc) return rc; }
     if (params_dirty_) { int rc = upload_params(); if (rc) return rc; }
     const bool graph = use_graph_ && !profiling_;
-    if (graph && (graph_dirty_ || !graph_exec_)) {
-        if (graph_exec_) { cudaGraphExecDestroy(graph_exec_); graph_exec_ = nullptr; }
-        if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
-        ENG_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
-        int rc = launch_substep(false);
-        cudaGraph_t g = nullptr;
-        cudaError_t ce = cudaStreamEndCapture(stream_, &g);
-        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
-        ENG_CK(ce, "end capture");
-        graph_ = g;
-        ENG_CK(cudaGraphInstantiate(&graph_exec_, graph_, 0), "graph instantiate");
+    if (graph && (graph_dirty_ || !exec_pre_ || !exec_suf_)) {
+        if (exec_pre_) { cudaGraphExecDestroy(exec_pre_); exec_pre_ = nullptr; }
+        if (exec_suf_) { cudaGraphExecDestroy(exec_suf_); exec_suf_ = nullptr; }
+        if (graph_pre_) { cudaGraphDestroy(graph_pre_); graph_pre_ = nullptr; }
+        if (graph_suf_) { cudaGraphDestroy(graph_suf_); graph_suf_ = nullptr; }
+        for (int half = 0; half < 2; ++half) {
+            ENG_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
+            int rc = half == 0 ? launch_prefix(false) : launch_suffix(false);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(stream_, &g);
+            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+            ENG_CK(ce, "end capture");
+            (half == 0 ? graph_pre_ : graph_suf_) = g;
+            ENG_CK(cudaGraphInstantiate(half == 0 ? &exec_pre_ : &exec_suf_, g, 0), "graph instantiate");
+        }
         graph_dirty_ = false;
     }
+    return ENG_OK;
+}
+
+int Engine::step(uint32_t substeps, bool sync) {
+    cudaSetDevice(device_);
+    if (scenes_.empty()) return ENG_OK;
+    if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
+    int rc = prepare();
+    if (rc) return rc;
+    const bool graph = use_graph_ && !profiling_;
     for (uint32_t s = 0; s < substeps; ++s) {
         if (graph) {
-            ENG_CK(cudaGraphLaunch(graph_exec_, stream_), "graph launch");
+            if (!prefix_valid_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+            ENG_CK(cudaGraphLaunch(exec_suf_, stream_), "graph launch");
         } else if (profiling_) {
-            int rc = launch_substep(true);
+            // a prefix computed for a state read is recomputed (same values) so
+            // that every pass of the substep is timed
+            rc = launch_prefix(true);
+            if (rc) return rc;
+            rc = launch_suffix(true);
             if (rc) return rc;
             ENG_CK(cudaEventSynchronize(ev_[7]), "profile sync");
             for (int i = 0; i < 7; ++i) {
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, ev_[i], ev_[i + 1]);
-                // pass i spans events i..i+1, except that pass 0 includes the memset
+                // pass i spans events i..i+1, except that pass 0 includes the memsets
                 pass_ms_[i] += ms;
             }
             float tot = 0.f;
@@ -521,12 +597,62 @@ int Engine::step(uint32_t substeps, bool sync) {
             pass_ms_[7] += tot;
             prof_substeps_++;
         } else {
-            int rc = launch_substep(false);
+            if (!prefix_valid_) { rc = launch_prefix(false); if (rc) return rc; }
+            rc = launch_suffix(false);
             if (rc) return rc;
         }
+        prefix_valid_ = false;
     }
+    for (auto& s : scenes_) s.pending = scene_defers(s);
     stepped_ = true;
     if (sync) return read_status();
+    return ENG_OK;
+}
+
+// Run the next substep's prefix once, for reads of scenes whose XSPH update
+// is pending: its density pass computes the updated velocities (Vc); the next
+// step() starts from the suffix, so the work is not repeated.
+int Engine::ensure_prefix() {
+    if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
+    if (prefix_valid_) return ENG_OK;
+    int rc = prepare();
+    if (rc) return rc;
+    if (use_graph_ && !profiling_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+    else { rc = launch_prefix(false); if (rc) return rc; }
+    rc = read_status();
+    if (rc) return rc;
+    prefix_valid_ = true;
+    return ENG_OK;
+}
+
+// Write a pending XSPH update into the state (V0) and clear it.  A fresh
+// prefix computes the same velocities from the updated state, so the prefix
+// stays valid.
+int Engine::materialize(Scene& s) {
+    if (!s.pending) return ENG_OK;
+    int rc = ensure_prefix();
+    if (rc) return rc;
+    const StepArgs a = args();
+    ENG_CK(launch_unsort_vel(a, s.tile_first, s.tile_count, s.part_base, nullptr, V0_, true, stream_), "materialize");
+    ENG_CK(cudaStreamSynchronize(stream_), "materialize sync");
+    s.pending = false;
+    return ENG_OK;
+}
+
+int Engine::materialize_all() {
+    for (auto& s : scenes_) {
+        int rc = materialize(s);
+        if (rc) return rc;
+    }
+    return ENG_OK;
+}
+
+int Engine::set_deferred_xsph(bool on) {
+    if (on == defer_xsph_) return ENG_OK;
+    if (!on) { int rc = materialize_all(); if (rc) return rc; }
+    defer_xsph_ = on;
+    params_dirty_ = true;
+    prefix_valid_ = false;
     return ENG_OK;
 }
 
@@ -564,9 +690,20 @@ int Engine::get_pass_times(double* ms_out, int cap, uint64_t* launches) {
     return ENG_OK;
 }
 
+void Engine::clear_pending(Scene& s) {
+    s.pending = false;
+    if (!layout_dirty_ && pend_ && s.table_index < pend_cap_) cudaMemsetAsync(pend_ + s.table_index, 0, sizeof(uint32_t), stream_);
+    prefix_valid_ = false;
+}
+
+Scene* Engine::mscene(int id) {
+    for (auto& s : scenes_) if (s.id == id) return &s;
+    return nullptr;
+}
+
 int Engine::set_state(int id, const float* pos, const float* vel, uint32_t n, bool from_device) {
     cudaSetDevice(device_);
-    const Scene* s = scene(id);
+    Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
     const float* dpos = pos;
@@ -584,6 +721,7 @@ int Engine::set_state(int id, const float* pos, const float* vel, uint32_t n, bo
             dvel = st + (size_t)n * 3;
         }
     }
+    clear_pending(*s);
     ENG_CK(launch_unpack(dpos, dvel, n, s->part_base, P0_, V0_, A0_, S_, stream_), "unpack");
     ENG_CK(cudaStreamSynchronize(stream_), "upload sync");
     return ENG_OK;
@@ -591,10 +729,13 @@ int Engine::set_state(int id, const float* pos, const float* vel, uint32_t n, bo
 
 int Engine::set_positions(int id, uint32_t first, const float* pos, uint32_t count) {
     cudaSetDevice(device_);
-    const Scene* s = scene(id);
+    Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if ((uint64_t)first + count > s->n) return fail(ENG_EINVAL, "range exceeds the scene's particle count");
     if (count == 0) return ENG_OK;
+    // the other particles keep their velocities: apply a pending XSPH update first
+    if (s->pending) { int rc = materialize(*s); if (rc) return rc; }
+    prefix_valid_ = false;
     const size_t bytes = (size_t)count * 3 * sizeof(float);
     float* st = nullptr;
     int rc = staging(bytes, &st);
@@ -607,21 +748,32 @@ int Engine::set_positions(int id, uint32_t first, const float* pos, uint32_t cou
 
 int Engine::generate_lattice(int id, const LatticeSpec& spec, uint32_t first) {
     cudaSetDevice(device_);
-    const Scene* s = scene(id);
+    Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     const uint64_t n = (uint64_t)spec.nx * spec.ny * spec.nz;
     if (first + n > s->n) return fail(ENG_EINVAL, "lattice exceeds the scene's particle count");
+    if (s->pending) { int rc = materialize(*s); if (rc) return rc; }
+    prefix_valid_ = false;
     ENG_CK(launch_lattice(spec, s->part_base + first, P0_, V0_, A0_, S_, stream_), "lattice");
     return ENG_OK;
 }
 
 int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n, bool to_device) {
     cudaSetDevice(device_);
-    const Scene* s = scene(id);
+    Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
+    // A pending XSPH update: the next substep's prefix computes the updated
+    // velocities (cell order), read back into state order; the state itself
+    // is not changed, so reading never alters the trajectory.
+    const bool pend = s->pending && vel;
+    if (pend) { int rc = ensure_prefix(); if (rc) return rc; }
+    const StepArgs a = args();
     if (to_device) {
-        ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, pos, colour, vel, stream_), "pack");
+        ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, pos, colour, pend ? nullptr : vel,
+                           stream_), "pack");
+        if (pend) ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, vel, nullptr, false,
+                                           stream_), "unsort");
         ENG_CK(cudaStreamSynchronize(stream_), "pack sync");
         return ENG_OK;
     }
@@ -635,7 +787,10 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     float* dp = pos ? st : nullptr;
     float* dc = colour ? st + (size_t)n * 3 : nullptr;
     float* dv = vel ? st + (size_t)n * 6 : nullptr;
-    ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, dv, stream_), "pack");
+    ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, pend ? nullptr : dv, stream_),
+           "pack");
+    if (pend) ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, dv, nullptr, false, stream_),
+                     "unsort");
     if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, stream_), "download");
     if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, stream_), "download");
     if (vel) ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
@@ -645,10 +800,13 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
 
 int Engine::save_state(int id, float4* host, uint32_t n) {
     cudaSetDevice(device_);
-    const Scene* s = scene(id);
+    Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
     if (n == 0) return ENG_OK;
+    // the snapshot holds a final state: apply a pending XSPH update (the
+    // values are those the next substep would use, so the run continues alike)
+    if (s->pending) { int rc = materialize(*s); if (rc) return rc; }
     const size_t bytes = (size_t)n * sizeof(float4);
     ENG_CK(cudaMemcpyAsync(host, P0_ + s->part_base, bytes, cudaMemcpyDeviceToHost, stream_), "snapshot");
     ENG_CK(cudaMemcpyAsync(host + n, V0_ + s->part_base, bytes, cudaMemcpyDeviceToHost, stream_), "snapshot");
@@ -660,10 +818,11 @@ int Engine::save_state(int id, float4* host, uint32_t n) {
 
 int Engine::load_state(int id, const float4* host, uint32_t n) {
     cudaSetDevice(device_);
-    const Scene* s = scene(id);
+    Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
     if (n == 0) return ENG_OK;
+    clear_pending(*s);
     const size_t bytes = (size_t)n * sizeof(float4);
     ENG_CK(cudaMemcpyAsync(P0_ + s->part_base, host, bytes, cudaMemcpyHostToDevice, stream_), "restore");
     ENG_CK(cudaMemcpyAsync(V0_ + s->part_base, host + n, bytes, cudaMemcpyHostToDevice, stream_), "restore");
@@ -676,8 +835,12 @@ int Engine::load_state(int id, const float4* host, uint32_t n) {
 
 int Engine::debug_enable(bool on) {
     if (on == debug_) return ENG_OK;
+    // debug taps show each substep's own passes: XSPH runs in every substep
+    if (on) { int rc = materialize_all(); if (rc) return rc; }
     debug_ = on;
     graph_dirty_ = true;
+    params_dirty_ = true;
+    prefix_valid_ = false;
     if (on && pcap_) {
         ENG_CK(cudaMalloc((void**)&dbg_nbr_, pcap_ * sizeof(uint32_t)), "debug alloc");
         ENG_CK(cudaMalloc((void**)&dbg_forces_, pcap_ * 4 * sizeof(float4)), "debug alloc");

@@ -44,6 +44,11 @@ struct Scene {
     uint32_t part_base = 0, n = 0;
     SceneConfig cfg;
     DevParams dp{};
+    // Its last substep's XSPH update is not yet applied to the state: the
+    // next density pass applies it (deferred XSPH).
+    bool pending = false;
+    // position in the device scene table and its tiles, as of the last layout
+    uint32_t table_index = 0, tile_first = 0, tile_count = 0;
 };
 
 enum { ENG_OK = 0, ENG_EINVAL = 1, ENG_ENOMEM = 2, ENG_ECUDA = 3, ENG_ENAN = 4, ENG_ECELL = 7 };
@@ -83,6 +88,16 @@ public:
                  F_FPRESSURE, F_FTENSION, F_FADHESION, F_FVISCOSITY, F_NORMAL, F_POS_SORTED, F_ACC, F_VEL_INT };
     int debug_get(int id, int field, void* host, uint64_t count);
 
+    // XSPH schedule.  Deferred (the default): a substep ends after the
+    // integrator and its XSPH update is applied by the next substep's density
+    // pass, fused into that walk; reading a scene's state (export, snapshot)
+    // first runs the next substep's sort and density pass, whose result the
+    // next step reuses, so reading never changes the trajectory.  Otherwise
+    // (and always with debug taps on, or for grids above SPH_OKEY_MAX_DIM cells
+    // per axis) every substep runs its own XSPH pass, as the reference does.
+    int set_deferred_xsph(bool on);
+    bool deferred_xsph() const { return defer_xsph_; }
+
     // Options.
     void set_use_graph(bool on) { use_graph_ = on; graph_dirty_ = true; }
     int set_exec(const ExecConfig& e);
@@ -115,7 +130,18 @@ private:
     int ensure_capacity(uint64_t parts, uint64_t cells);
     int rebuild_layout();
     int upload_params();
-    int launch_substep(bool profile);
+    int launch_prefix(bool profile);   // memsets, hash, scan, sort, density
+    int launch_suffix(bool profile);   // normals, force + integrator, [XSPH]
+    int ensure_prefix();               // the next substep's prefix, computed once
+    int materialize(Scene& s);         // apply a pending XSPH update to the state
+    int materialize_all();
+    void clear_pending(Scene& s);      // state replaced: nothing pending
+    Scene* mscene(int id);
+    bool scene_defers(const Scene& s) const {
+        return defer_xsph_ && !debug_ && s.dp.gx <= SPH_OKEY_MAX_DIM && s.dp.gy <= SPH_OKEY_MAX_DIM &&
+               s.dp.gz <= SPH_OKEY_MAX_DIM;
+    }
+    int prepare();                     // layout, params and graphs up to date
     int read_status();
     void free_all();
     uint32_t alloc_slots(uint32_t n);
@@ -133,7 +159,9 @@ private:
     uint64_t pcap_ = 0, ccap_ = 0, slots_end_ = 0;
     // device arenas
     float4 *P0_ = nullptr, *P1_ = nullptr, *V0_ = nullptr, *V1_ = nullptr, *V2_ = nullptr, *A0_ = nullptr,
-           *A1_ = nullptr, *S_ = nullptr, *N_ = nullptr;
+           *A1_ = nullptr, *S_ = nullptr, *N_ = nullptr, *Vc_ = nullptr;
+    uint32_t *okey_ = nullptr, *okey1_ = nullptr;   // packed cells: last substep (state), gathered
+    uint32_t *pend_ = nullptr;                      // per scene-table entry: XSPH update pending
     uint32_t *key_ = nullptr, *slot_ = nullptr, *tmp_ = nullptr, *perm_ = nullptr;
     uint32_t *count_ = nullptr, *start_ = nullptr, *scan_sums_ = nullptr, *status_ = nullptr;
     uint32_t *mask_ = nullptr;        // 9 neighbour-mask words per slot
@@ -161,8 +189,12 @@ private:
     bool layout_dirty_ = true, params_dirty_ = true, graph_dirty_ = true;
     bool debug_ = false, use_graph_ = true, profiling_ = false;
     bool stepped_ = false;
-    cudaGraph_t graph_ = nullptr;
-    cudaGraphExec_t graph_exec_ = nullptr;
+    bool defer_xsph_ = true;
+    bool all_defer_ = false;           // every scene defers: no XSPH pass in the substep
+    uint64_t pend_cap_ = 0;
+    bool prefix_valid_ = false;        // the next substep's prefix has run (for a state read)
+    cudaGraph_t graph_pre_ = nullptr, graph_suf_ = nullptr;
+    cudaGraphExec_t exec_pre_ = nullptr, exec_suf_ = nullptr;
     cudaEvent_t ev_[kPasses + 1] = {};
     cudaEvent_t timers_[64] = {};
     double pass_ms_[kPasses] = {};

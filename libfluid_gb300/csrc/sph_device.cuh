@@ -91,6 +91,28 @@ __device__ __forceinline__ uint32_t cell_of(const DevParams& P, float x, float y
     return grid_inside(P, g) ? (uint32_t)g.x + (uint32_t)g.y * P.gx + (uint32_t)g.z * P.gxy : P.ncells;
 }
 
+// A particle's cell packed as x | y << 10 | z << 20 (grids of at most 1024
+// cells per axis; larger grids run XSPH every substep), or SPH_OKEY_NULL
+// outside the grid.  Kept from one substep to the next for deferred XSPH.
+__device__ __forceinline__ uint32_t pack_cell(int3 g) {
+    return (uint32_t)g.x | ((uint32_t)g.y << 10) | ((uint32_t)g.z << 20);
+}
+// Both packed cells exist and differ by at most one in every axis (one is in
+// the other's 27-cell neighbourhood).  Bit 31 (SPH_OKEY_MOVED) is ignored.
+__device__ __forceinline__ bool cells_adjacent(uint32_t a, uint32_t b) {
+    if (b == SPH_OKEY_NULL) return false;
+    const int dx = (int)(a & 1023u) - (int)(b & 1023u);
+    const int dy = (int)((a >> 10) & 1023u) - (int)((b >> 10) & 1023u);
+    const int dz = (int)((a >> 20) & 1023u) - (int)((b >> 20) & 1023u);
+    return (unsigned)(dx + 1) <= 2u && (unsigned)(dy + 1) <= 2u && (unsigned)(dz + 1) <= 2u;
+}
+// The same for a pair already known to lie in each other's current 27-cell
+// neighbourhood: when neither particle changed cell (no SPH_OKEY_MOVED bit,
+// set by the hash pass), the previous cells are the current ones.
+__device__ __forceinline__ bool cells_adjacent_fast(uint32_t a, uint32_t b) {
+    return ((a | b) & SPH_OKEY_MOVED) == 0u || cells_adjacent(a, b);
+}
+
 // Visit the candidate neighbours of a particle in grid cell g: the 27 cells
 // around it, clipped at the grid edge (fluidphysics.cu:30-34).  Cells
 // (x-1..x+1, y, z) are consecutive in the x-fastest order and particles are

@@ -25,13 +25,16 @@ namespace sph {
 // fluidsystem.cu:304-306).  Equal keys inside a warp are combined with
 // __match_any_sync so one atomic serves each group; the slot a particle gets
 // inside its cell is provisional (atomic order) and is made stable by
-// k_rank_gather.
+// k_rank_gather.  For a scene with a pending XSPH update, a particle whose
+// cell differs from the one recorded by the last force pass gets the
+// SPH_OKEY_MOVED flag there (the density pass's fast adjacency test).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(SPH_TILE) k_hash(const DevParams* __restrict__ params,
                                                    const DevScene* __restrict__ scenes,
                                                    const uint4* __restrict__ tiles,
                                                    const float4* __restrict__ P, uint32_t* __restrict__ count,
                                                    uint32_t* __restrict__ key, uint32_t* __restrict__ slot,
+                                                   const uint32_t* __restrict__ pend, uint32_t* __restrict__ okey,
                                                    uint32_t* __restrict__ status) {
     const uint4 t = tiles[blockIdx.x];
     if (threadIdx.x >= t.z) return;
@@ -39,7 +42,13 @@ __global__ void __launch_bounds__(SPH_TILE) k_hash(const DevParams* __restrict__
     const DevScene sc = scenes[t.x];
     const DevParams& pp = params[t.x];
     const float4 p = P[i];
-    const uint32_t local = cell_of(pp, p.x, p.y, p.z);
+    const int3 gc = grid_of(pp, p.x, p.y, p.z);
+    const bool inside = grid_inside(pp, gc);
+    const uint32_t local = inside ? (uint32_t)gc.x + (uint32_t)gc.y * pp.gx + (uint32_t)gc.z * pp.gxy : pp.ncells;
+    if (__ldg(pend + t.x) != 0u) {
+        const uint32_t o = okey[i];
+        if (o != SPH_OKEY_NULL && (!inside || (o & ~SPH_OKEY_MOVED) != pack_cell(gc))) okey[i] = o | SPH_OKEY_MOVED;
+    }
     if (!(isfinite(p.x) && isfinite(p.y) && isfinite(p.z))) atomicOr(status, SPH_STATUS_NONFINITE);
     const uint32_t gkey = sc.cell_base + local;
     const unsigned lane = threadIdx.x & 31u;
@@ -178,6 +187,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_scatter(const DevScene* __restrict
 // particles keep their current order.  Each sorted slot's final position is
 // the cell start plus the number of cell members with a smaller current
 // index, which reproduces that permutation exactly.
+// A scene whose last XSPH update is still pending (pend[scene] != 0) has its
+// post-integration velocities in V2 and its previous cells in okey: those
+// are gathered (the density pass applies the XSPH update); otherwise V0.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __restrict__ scenes,
                                                           const uint4* __restrict__ tiles,
@@ -187,13 +199,18 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
                                                           const float4* __restrict__ P0,
                                                           const float4* __restrict__ V0,
                                                           const float4* __restrict__ A0,
+                                                          const float4* __restrict__ V2,
+                                                          const uint32_t* __restrict__ okey,
+                                                          const uint32_t* __restrict__ pend,
                                                           float4* __restrict__ P1, float4* __restrict__ V1,
-                                                          float4* __restrict__ A1, uint32_t* __restrict__ perm,
+                                                          float4* __restrict__ A1, uint32_t* __restrict__ okey1,
+                                                          uint32_t* __restrict__ perm,
                                                           uint32_t* __restrict__ status) {
     const uint4 t = tiles[blockIdx.x];
     if (threadIdx.x >= t.z) return;
     const uint32_t g = t.y + threadIdx.x;
     const DevScene sc = scenes[t.x];
+    const bool pending = __ldg(pend + t.x) != 0u;
     const uint32_t i = tmp[g];
     const uint32_t s0 = __ldg(start + sc.cell_base);
     const uint32_t c = sc.cell_base + __ldg(key + i);
@@ -208,8 +225,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
     const uint32_t f = b + rank;
     perm[f] = i;
     P1[f] = P0[i];
-    V1[f] = V0[i];
+    V1[f] = pending ? V2[i] : V0[i];
     A1[f] = A0[i];
+    if (pending) okey1[f] = __ldg(okey + i);
 }
 
 // ---------------------------------------------------------------------------
@@ -218,14 +236,32 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // with two loads in flight (1); the candidates and their order are the same.
 // (A flattened loop over a row table in shared memory measured slower here:
 // 64 registers against 48.)
+//
+// Deferred XSPH.  For a scene whose previous substep ended without its XSPH
+// update (pend[scene] != 0), P1 holds that substep's post-integration
+// positions (w = its densities), V1 its post-integration velocities and okey1
+// the cells the particles were sorted into then.  The reference's update
+// (correctVelocityXSPH, fluidphysics.cu:355-409) sums over pairs with
+// r^2 <= h^2 at these positions whose previous cells are adjacent (its cell
+// lists were those of the previous sort); every such pair is within h now, so
+// this candidate walk meets all of them, and the previous-cell test keeps
+// exactly the reference's pairs.  The poly6 weight is the one the density sum
+// just computed.  The corrected velocity goes to Vc, which the force pass
+// reads; without a pending update Vc = V1.
 // ---------------------------------------------------------------------------
+#ifndef DENSITY_MINB
+#define DENSITY_MINB 4
+#endif
 template <int WALK>
-__global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restrict__ params,
+__global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevParams* __restrict__ params,
                                                       const DevScene* __restrict__ scenes,
                                                       const uint4* __restrict__ tiles,
                                                       const uint32_t* __restrict__ start,
                                                       const float4* __restrict__ P1, float4* __restrict__ S,
                                                       uint32_t* __restrict__ mask, size_t mask_stride,
+                                                      const float4* __restrict__ V1,
+                                                      const uint32_t* __restrict__ okey1,
+                                                      const uint32_t* __restrict__ pend, float4* __restrict__ Vc,
                                                       uint32_t* __restrict__ nbr_out, uint32_t ntiles,
                                                       uint32_t* __restrict__ tile_ctr) {
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
@@ -234,9 +270,11 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
     const DevScene sc = scenes[t.x];
     const DevParams& pp = params[t.x];
     const float4 p = P1[k];
+    const float4 vi = V1[k];
     const int3 g = grid_of(pp, p.x, p.y, p.z);
     if (!grid_inside(pp, g)) {
         S[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        Vc[k] = vi;
         if (nbr_out) nbr_out[k] = 0;
         return;
     }
@@ -244,6 +282,39 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
     const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = pp.skin2, eps = pp.eps;
     float sum = 0.0f;
     uint32_t cnt = 0;
+    // deferred XSPH of the previous substep (only for particles that had a cell then)
+    const uint32_t oi = (__ldg(pend + t.x) != 0u) ? __ldg(okey1 + k) : SPH_OKEY_NULL;
+    const bool xs = oi != SPH_OKEY_NULL;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    // One XSPH pair term of the pending update, given the pair's poly6 weight.
+    auto xsph_term = [&](const float4& q, const float4& vj, uint32_t oj, float w) {
+        const float rs = p.w + q.w;   // the previous substep's densities
+        if (rs > eps && cells_adjacent_fast(oi, oj)) {
+            const float coeff = w * __fdividef(pp.two_mass, rs);
+            ax = fmaf(coeff, vj.x - vi.x, ax);
+            ay = fmaf(coeff, vj.y - vi.y, ay);
+            az = fmaf(coeff, vj.z - vi.z, az);
+        }
+    };
+    // The pending update's pairs of one row, right after the row's candidate
+    // scan (their positions are still in L1): the neighbours just recorded
+    // (eps < r^2 <= h^2, offsets below 32), each pair's loads issued together.
+    // The few pairs the row word cannot hold are taken inline in the scan.
+    auto xsph_row = [&](uint32_t jb0, uint32_t be0) {
+        while (be0) {
+            const int b = __ffs(be0) - 1;
+            be0 &= be0 - 1u;
+            const uint32_t j = jb0 + (uint32_t)b;
+            const float4 q = __ldg(P1 + j), vj = __ldg(V1 + j);
+            const uint32_t oj = __ldg(okey1 + j);
+            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+            const float rr = dot3(dx, dy, dz, dx, dy, dz);
+            const float rd = sqrtf(rr);
+            const float x = fmaf(-rd, rd, h2);
+            const float w = (rd >= h) ? 0.0f : c6 * (x * x * x);
+            xsph_term(q, vj, oj, w);
+        }
+    };
     // Every candidate is tested here and recorded per row for the later
     // passes: mask words 0-8 hold the candidates within the skin radius
     // (XSPH), words 9-17 the exact neighbours j != i, eps < r^2 <= h^2 (the
@@ -262,6 +333,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
                 const float w = (rd >= h) ? 0.0f : c6 * (x * x * x);
                 sum = fmaf(mass, w, sum);
                 cnt++;
+                // XSPH pairs outside the row word: coincident particles and
+                // offsets of 32 and beyond
+                if (xs && (rr <= eps || off >= 32u)) xsph_term(q, __ldg(V1 + jj), __ldg(okey1 + jj), w);
             }
         }
     };
@@ -279,6 +353,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
                 if (jj < je0) visit(__ldg(P1 + jj), jj, jb0, bs0, be0);
                 mask[(size_t)rr * mask_stride + k] = bs0;
                 mask[(size_t)(9 + rr) * mask_stride + k] = be0;
+                if (xs) xsph_row(jb0, be0);
             }
         }
     } else {
@@ -291,6 +366,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
                 if (valid) {
                     mask[(size_t)r * mask_stride + k] = bs;
                     mask[(size_t)(9 + r) * mask_stride + k] = be;
+                    if (xs) xsph_row(jb, be);
                 }
                 if (++r >= 9) break;
                 bs = be = 0u;
@@ -312,6 +388,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_density(const DevParams* __restric
     const float cs = pp.gas_constant * powf(ratio, pp.gamma - 1.0f);
     // w = 1/rho^2, used by the force pass for p_j/rho_i^2 + p_i/rho_j^2
     S[k] = make_float4(rho, prs, cs, 1.0f / (rho * rho));
+    Vc[k] = xs ? make_float4(fmaf(pp.xsph, ax, vi.x), fmaf(pp.xsph, ay, vi.y), fmaf(pp.xsph, az, vi.z), 0.f) : vi;
     if (nbr_out) nbr_out[k] = cnt;
   });
 }
@@ -386,8 +463,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
 // ---------------------------------------------------------------------------
 // Forces (computeAllForces, fluidphysics.cu:215-352) fused with the leapfrog
 // integrator and box boundary (LeapfrogIntegratorOperator,
-// fluidintegrator.cu:11-70).  Reads cell-order state (P1,V1,A1,S,N), writes
-// the integrated state to P0 (w = density), V2, A0.  The integrator sums the
+// fluidintegrator.cu:11-70).  Reads cell-order state (P1, the velocities Vc
+// of the density pass (V1 with any pending XSPH update applied) through the
+// V1 argument, A1, S, N), writes the integrated state to P0 (w = density), V2,
+// A0, and each particle's cell to okey.  The integrator sums the
 // force buffers in the reference's order, which after the swapped arguments
 // at fluidsystem.cu:352-364 is ((pressure + tension) + viscosity) + adhesion.
 // ---------------------------------------------------------------------------
@@ -410,6 +489,7 @@ k_force_integrate(const DevParams* __restrict__ params,
                                                               const uint32_t* __restrict__ mask, size_t mask_stride,
                                                               float4* __restrict__ P0, float4* __restrict__ V2,
                                                               float4* __restrict__ A0, uint32_t* __restrict__ maxdisp,
+                                                              uint32_t* __restrict__ okey, uint32_t* __restrict__ pend,
                                                               float4* __restrict__ dbg_forces, uint32_t ntiles,
                                                               uint32_t* __restrict__ tile_ctr) {
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
@@ -419,6 +499,9 @@ k_force_integrate(const DevParams* __restrict__ params,
     const uint32_t k = t.y + threadIdx.x;
     const DevScene sc = scenes[t.x];
     const DevParams& pp = params[t.x];
+    // the scene's XSPH update is now pending (applied by the next density
+    // pass, or by k_xsph right after this pass)
+    if (threadIdx.x == 0) pend[t.x] = 1u;
     const float4 pi = P1[k];
     const float4 vi = V1[k];
     const float4 si = S[k];
@@ -543,6 +626,7 @@ k_force_integrate(const DevParams* __restrict__ params,
     P0[k] = make_float4(px, py, pz, si.x);
     V2[k] = make_float4(vx, vy, vz, 0.f);
     A0[k] = make_float4(anx, any, anz, 0.f);
+    okey[k] = grid_inside(pp, g) ? pack_cell(g) : SPH_OKEY_NULL;   // the cell XSPH's cell lists use
     // largest displacement of the substep in units of h (squared), for XSPH's
     // use of the neighbour masks; NaN compares above every finite value
     const float ddx = px - pi.x, ddy = py - pi.y, ddz = pz - pi.z;
@@ -594,12 +678,15 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
                                                    const float4* __restrict__ V2,
                                                    const uint32_t* __restrict__ mask, size_t mask_stride,
                                                    const uint32_t* __restrict__ maxdisp, float4* __restrict__ V0,
-                                                   uint32_t ntiles, uint32_t* __restrict__ tile_ctr) {
+                                                   uint32_t* __restrict__ pend, uint32_t ntiles,
+                                                   uint32_t* __restrict__ tile_ctr) {
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
     const DevScene sc = scenes[t.x];
     const DevParams& pp = params[t.x];
+    if (pp.flags & SPH_FLAG_DEFER_XSPH) return;   // the next density pass applies it
+    if (threadIdx.x == 0) pend[t.x] = 0u;         // the update is applied here
     const float4 vi = V2[k];
     const float4 old = P1[k];   // the cell this particle was sorted into
     const int3 g = grid_of(pp, old.x, old.y, old.z);
@@ -629,6 +716,32 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
     }
     V0[k] = make_float4(fmaf(pp.xsph, sx, vi.x), fmaf(pp.xsph, sy, vi.y), fmaf(pp.xsph, sz, vi.z), 0.f);
   });
+}
+
+// ---------------------------------------------------------------------------
+// The velocities of a density pass (Vc, cell order) back in the state order
+// of the substep before it (slot perm[f]): the export of a scene whose XSPH
+// update was pending (packed xyz into `out`, particle perm[f] - base), and its
+// materialisation into the state (V0, clearing the scene's pending flag).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_unsort_vel(const uint4* __restrict__ tiles,
+                                                         const uint32_t* __restrict__ perm,
+                                                         const float4* __restrict__ Vc, uint32_t base,
+                                                         float* __restrict__ out, float4* __restrict__ V0,
+                                                         uint32_t* __restrict__ pend) {
+    const uint4 t = tiles[blockIdx.x];
+    if (pend && blockIdx.x == 0 && threadIdx.x == 0) pend[t.x] = 0u;
+    if (threadIdx.x >= t.z) return;
+    const uint32_t f = t.y + threadIdx.x;
+    const uint32_t i = __ldg(perm + f);
+    const float4 v = Vc[f];
+    if (out) {
+        const size_t o = 3 * (size_t)(i - base);
+        out[o] = v.x;
+        out[o + 1] = v.y;
+        out[o + 2] = v.z;
+    }
+    if (V0) V0[i] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -712,7 +825,8 @@ __global__ void k_sorted_keys(const uint32_t* __restrict__ key, const uint32_t* 
 // Launch wrappers.
 // ---------------------------------------------------------------------------
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st) {
-    k_hash<<<a.ntiles, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.P0, a.count, a.key, a.slot, a.status);
+    k_hash<<<a.ntiles, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.P0, a.count, a.key, a.slot, a.pend, a.okey,
+                                         a.status);
     return cudaGetLastError();
 }
 static inline uint32_t* ctr(const StepArgs& a, int k) { return a.tile_ctr ? a.tile_ctr + k : nullptr; }
@@ -754,14 +868,21 @@ cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_s
 }
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
     k_scatter<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
-    k_rank_gather<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.P1,
-                                                a.V1, a.A1, a.perm, a.status);
+    k_rank_gather<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.V2,
+                                                a.okey, a.pend, a.P1, a.V1, a.A1, a.okey1, a.perm, a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
     auto kern = (a.variant & SPH_VARIANT_DENSITY_ROWS) ? k_density<1> : k_density<0>;
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
-                                         a.dbg_nbr, a.ntiles, ctr(a, 0));
+                                         a.V1, a.okey1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
+    return cudaGetLastError();
+}
+cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,
+                              float4* V0, bool clear_pending, cudaStream_t st) {
+    if (ntiles == 0) return cudaSuccess;
+    k_unsort_vel<<<ntiles, a.block, 0, st>>>(a.tiles + first_tile, a.perm, a.Vc, base, out, V0,
+                                             clear_pending ? a.pend : nullptr);
     return cudaGetLastError();
 }
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
@@ -781,15 +902,15 @@ cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
                     : (table ? (occ ? k_force_integrate<false, 4, true> : k_force_integrate<false, 3, true>)
                              : (occ ? k_force_integrate<false, 4, false> : k_force_integrate<false, 3, false>));
     const size_t smem = table ? (size_t)18 * a.block * sizeof(uint32_t) : 0;
-    kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.V1, a.A1, a.S, a.N, a.mask,
-                                         a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp, a.dbg_forces, a.ntiles,
-                                         ctr(a, 2));
+    kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.Vc, a.A1, a.S, a.N, a.mask,
+                                            a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp, a.okey, a.pend, a.dbg_forces,
+                                            a.ntiles, ctr(a, 2));
     return cudaGetLastError();
 }
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st) {
     auto kern = (a.variant & SPH_VARIANT_XSPH_ROWS) ? k_xsph<1> : k_xsph<0>;
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.mask,
-                                         a.mask_stride, a.maxdisp, a.V0, a.ntiles, ctr(a, 3));
+                                         a.mask_stride, a.maxdisp, a.V0, a.pend, a.ntiles, ctr(a, 3));
     return cudaGetLastError();
 }
 cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,

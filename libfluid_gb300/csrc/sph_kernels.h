@@ -15,7 +15,10 @@ struct StepArgs {
     uint32_t total_cells;      // packed cell arena size including NULL buckets
     float4 *P0, *V0, *A0;      // state
     float4 *P1, *V1, *A1;      // cell-ordered state
-    float4 *V2;                // post-integration velocity
+    float4 *V2;                // post-integration velocity (before XSPH)
+    float4 *Vc;                // cell-ordered velocities with any pending XSPH update applied
+    uint32_t *okey, *okey1;    // each slot's cell in the last substep (packed), and gathered into cell order
+    uint32_t *pend;            // per scene: its last XSPH update is pending
     float4 *S;                 // (rho, p, c^2, 0)
     float4 *N;                 // normals
     uint32_t *count, *start, *scan_sums;
@@ -53,6 +56,11 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st);
+// Vc (cell order, over tiles [first_tile, first_tile + ntiles) of one scene)
+// back into state order: packed xyz into `out` (particle slot - base) and/or
+// into V0; optionally clears the scene's pending flag.
+cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,
+                              float4* V0, bool clear_pending, cudaStream_t st);
 
 cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,
                           float4* A0, float4* S, cudaStream_t st);

@@ -9,6 +9,10 @@
 #include <stdint.h>
 
 #define SPH_NULL_HASH 0xFFFFFFFFu   // fluiddefines.h:12 (UINT_MAX)
+#define SPH_OKEY_NULL 0xFFFFFFFFu   // packed cell of a particle outside the grid
+#define SPH_OKEY_MOVED 0x80000000u  // packed-cell flag: the particle has changed cell since
+#define SPH_OKEY_MAX_DIM 1024u      // grids up to this many cells per axis can defer XSPH
+#define SPH_FLAG_DEFER_XSPH 0x2u    // DevParams.flags: XSPH applied by the next density pass
 
 // Derived per-scene parameters (the FluidParamData of fluidparams.cuh:16-69,
 // generalised to a rectangular box [0,L]^3 with cell size h).
@@ -31,7 +35,8 @@ struct DevParams {
     float vel_limit, acc_limit, vel_limit2, acc_limit2;
     float grav_x, grav_y, grav_z;
     float eps;                    // FLT_MIN (fluidparams.cu:48)
-    uint32_t flags;               // bit0: surface tension active (normals pass needed)
+    uint32_t flags;               // bit0: surface tension active (normals pass needed);
+                                  // bit1: the scene defers XSPH (SPH_FLAG_DEFER_XSPH)
     float skin2;                  // ((1 + skin) h)^2: radius of the neighbour masks
     float inv_h2;                 // 1/h^2, normalises displacements for the XSPH mask check
     float xsph_disp_limit2;       // (skin/2)^2 * 0.98: largest (displacement/h)^2 XSPH may accept
