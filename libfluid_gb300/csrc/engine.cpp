@@ -489,6 +489,7 @@ StepArgs Engine::args() const {
     a.grid_nbr = exec_.persistent ? std::min<uint32_t>(a.ntiles, (uint32_t)sm_count_ * exec_.persistent) : a.ntiles;
     a.variant = exec_.variant;
     a.any_tension = any_tension_ ? 1u : 0u;
+    a.skin_masks = all_defer_ ? 0u : 1u;
     a.dbg_nbr = debug_ ? dbg_nbr_ : nullptr;
     a.dbg_forces = debug_ ? dbg_forces_ : nullptr;
     return a;

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 #ifndef DENSITY_MINB
 #define DENSITY_MINB 4
 #endif
-template <int WALK>
+template <int WALK, bool SKIN>
 __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevParams* __restrict__ params,
                                                       const DevScene* __restrict__ scenes,
                                                       const uint4* __restrict__ tiles,
@@ -279,7 +279,8 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         return;
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
-    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = pp.skin2, eps = pp.eps;
+    // the skin-radius masks serve only the per-substep XSPH pass
+    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = SKIN ? pp.skin2 : pp.h2, eps = pp.eps;
     float sum = 0.0f;
     uint32_t cnt = 0;
     // deferred XSPH of the previous substep (only for particles that had a cell then)
@@ -351,7 +352,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                     visit(q1, jj + 1u, jb0, bs0, be0);
                 }
                 if (jj < je0) visit(__ldg(P1 + jj), jj, jb0, bs0, be0);
-                mask[(size_t)rr * mask_stride + k] = bs0;
+                if (SKIN) mask[(size_t)rr * mask_stride + k] = bs0;
                 mask[(size_t)(9 + rr) * mask_stride + k] = be0;
                 if (xs) xsph_row(jb0, be0);
             }
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         for (;;) {
             if (j >= je) {
                 if (valid) {
-                    mask[(size_t)r * mask_stride + k] = bs;
+                    if (SKIN) mask[(size_t)r * mask_stride + k] = bs;
                     mask[(size_t)(9 + r) * mask_stride + k] = be;
                     if (xs) xsph_row(jb, be);
                 }
@@ -632,8 +633,10 @@ k_force_integrate(const DevParams* __restrict__ params,
     const float ddx = px - pi.x, ddy = py - pi.y, ddz = pz - pi.z;
     const float d2 = dot3(ddx, ddy, ddz, ddx, ddy, ddz) * pp.inv_h2;
     const uint32_t bits = (d2 != d2) ? 0x7fffffffu : __float_as_uint(d2);
-    const uint32_t wmax = __reduce_max_sync(lanes, bits);
-    if ((threadIdx.x & 31u) == (uint32_t)(__ffs(lanes) - 1)) atomicMax(maxdisp, wmax);
+    if (maxdisp) {   // only scenes with a per-substep XSPH pass use the skin masks
+        const uint32_t wmax = __reduce_max_sync(lanes, bits);
+        if ((threadIdx.x & 31u) == (uint32_t)(__ffs(lanes) - 1)) atomicMax(maxdisp, wmax);
+    }
   });
 }
 
@@ -873,7 +876,9 @@ cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
     return cudaGetLastError();
 }
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
-    auto kern = (a.variant & SPH_VARIANT_DENSITY_ROWS) ? k_density<1> : k_density<0>;
+    const bool rows = (a.variant & SPH_VARIANT_DENSITY_ROWS) != 0u;
+    auto kern = a.skin_masks ? (rows ? k_density<1, true> : k_density<0, true>)
+                             : (rows ? k_density<1, false> : k_density<0, false>);
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
                                          a.V1, a.okey1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
@@ -903,7 +908,8 @@ cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
                              : (occ ? k_force_integrate<false, 4, false> : k_force_integrate<false, 3, false>));
     const size_t smem = table ? (size_t)18 * a.block * sizeof(uint32_t) : 0;
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.Vc, a.A1, a.S, a.N, a.mask,
-                                            a.mask_stride, a.P0, a.V2, a.A0, a.maxdisp, a.okey, a.pend, a.dbg_forces,
+                                            a.mask_stride, a.P0, a.V2, a.A0, a.skin_masks ? a.maxdisp : nullptr,
+                                            a.okey, a.pend, a.dbg_forces,
                                             a.ntiles, ctr(a, 2));
     return cudaGetLastError();
 }

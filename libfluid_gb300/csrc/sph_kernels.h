@@ -33,6 +33,7 @@ struct StepArgs {
     uint32_t *tile_ctr;        // 4 tile counters for persistent neighbour passes, or nullptr
     uint32_t variant;          // SPH_VARIANT_* bits: per-row walks, force register budget
     uint32_t any_tension;      // nonzero when some live scene has surface tension on
+    uint32_t skin_masks;       // nonzero when some scene runs a per-substep XSPH pass (needs the skin masks)
     uint32_t *dbg_nbr;         // optional: neighbour counts per sorted slot
     float4 *dbg_forces;        // optional: 4 force vectors per sorted slot
 };
