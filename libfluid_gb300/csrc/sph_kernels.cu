@@ -2,16 +2,19 @@
 //
 // One substep (the body of FluidSystem::advance, fluidsystem.cu:301-398) is:
 //   memset counts -> k_hash -> scan (3 kernels) -> k_scatter -> k_rank_gather
-//   -> k_density -> [k_normals] -> k_force_integrate -> k_xsph
+//   -> k_density (+ the previous substep's XSPH update) -> [k_normals]
+//   -> k_force_integrate [-> k_xsph, for scenes that do not defer XSPH]
 // Every kernel is scene-aware: a launch covers the tiles of all live scenes,
 // so the plain step is the batched step with one scene.
 //
 // State buffers (float4 per particle, slots indexed by the arena):
 //   P0,V0,A0  state between substeps (P0.w = density of the last substep)
-//   P1,V1,A1  state gathered into cell order
-//   S         (rho, p, c^2, 0) per sorted slot
+//   V2, okey  post-integration velocity and cell of the last substep, for a
+//             scene whose XSPH update is pending (pend[scene] != 0)
+//   P1,V1,A1  state gathered into cell order (okey1: the gathered cells)
+//   S         (rho, p, c^2, 1/rho^2) per sorted slot
+//   Vc        cell-ordered velocities with the pending XSPH update applied
 //   N         surface normals (only when a scene has surface tension)
-//   V2        post-integration velocity (read by XSPH, which writes V0)
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "sph_types.h"
