@@ -499,8 +499,9 @@ StepArgs Engine::args() const {
 // (sort and density, with any pending XSPH update) ends where a state read
 // needs it; the suffix is the rest (normals, forces and integrator, and the
 // XSPH pass of scenes that do not defer it).
-int Engine::launch_prefix(bool profile) {
-    const StepArgs a = args();
+int Engine::launch_prefix(bool profile) { return launch_prefix_args(args(), profile); }
+
+int Engine::launch_prefix_args(const StepArgs& a, bool profile) {
     cudaStream_t st = stream_;
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     mark(0);
@@ -549,19 +550,31 @@ int Engine::prepare() {
     if (params_dirty_) { int rc = upload_params(); if (rc) return rc; }
     const bool graph = use_graph_ && !profiling_;
     if (graph && (graph_dirty_ || !exec_pre_ || !exec_suf_)) {
-        if (exec_pre_) { cudaGraphExecDestroy(exec_pre_); exec_pre_ = nullptr; }
-        if (exec_suf_) { cudaGraphExecDestroy(exec_suf_); exec_suf_ = nullptr; }
-        if (graph_pre_) { cudaGraphDestroy(graph_pre_); graph_pre_ = nullptr; }
-        if (graph_suf_) { cudaGraphDestroy(graph_suf_); graph_suf_ = nullptr; }
+        // Re-capture; when only launch sizes and arguments changed (scenes
+        // joined or left), update the instantiated graphs in place, which is
+        // much cheaper than instantiating again.
         for (int half = 0; half < 2; ++half) {
+            cudaGraph_t& gref = half == 0 ? graph_pre_ : graph_suf_;
+            cudaGraphExec_t& eref = half == 0 ? exec_pre_ : exec_suf_;
             ENG_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
             int rc = half == 0 ? launch_prefix(false) : launch_suffix(false);
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(stream_, &g);
             if (rc) { if (g) cudaGraphDestroy(g); return rc; }
             ENG_CK(ce, "end capture");
-            (half == 0 ? graph_pre_ : graph_suf_) = g;
-            ENG_CK(cudaGraphInstantiate(half == 0 ? &exec_pre_ : &exec_suf_, g, 0), "graph instantiate");
+            bool updated = false;
+            if (eref) {
+                cudaGraphExecUpdateResultInfo info;
+                updated = cudaGraphExecUpdate(eref, g, &info) == cudaSuccess;
+                if (!updated) {
+                    cudaGetLastError();   // the update's error is not sticky; instantiate instead
+                    cudaGraphExecDestroy(eref);
+                    eref = nullptr;
+                }
+            }
+            if (gref) cudaGraphDestroy(gref);
+            gref = g;
+            if (!updated) ENG_CK(cudaGraphInstantiate(&eref, g, 0), "graph instantiate");
         }
         graph_dirty_ = false;
     }
@@ -624,6 +637,24 @@ int Engine::ensure_prefix() {
     if (rc) return rc;
     prefix_valid_ = true;
     return ENG_OK;
+}
+
+// The prefix for one scene only (its tiles; every scene's cells are scanned,
+// the others hold no particles then): a read of one scene of many costs that
+// scene's share.  Scene-local, so its values equal a full prefix's; the full
+// prefix is not valid afterwards.
+int Engine::prefix_scene(const Scene& sc) {
+    int rc = prepare();
+    if (rc) return rc;
+    StepArgs a = args();
+    a.tiles = d_tiles_ + sc.tile_first;
+    a.ntiles = sc.tile_count;
+    a.grid_nbr = sc.tile_count;
+    a.tile_ctr = nullptr;
+    rc = launch_prefix_args(a, false);
+    if (rc) return rc;
+    prefix_valid_ = false;
+    return read_status();
 }
 
 // Write a pending XSPH update into the state (V0) and clear it.  A fresh
@@ -768,7 +799,12 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     // velocities (cell order), read back into state order; the state itself
     // is not changed, so reading never alters the trajectory.
     const bool pend = s->pending && vel;
-    if (pend) { int rc = ensure_prefix(); if (rc) return rc; }
+    if (pend) {
+        // one scene of several, and no full prefix at hand: that scene's prefix only
+        if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
+        int rc = (prefix_valid_ || scenes_.size() == 1) ? ensure_prefix() : prefix_scene(*s);
+        if (rc) return rc;
+    }
     const StepArgs a = args();
     if (to_device) {
         ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, pos, colour, pend ? nullptr : vel,

@@ -131,6 +131,8 @@ private:
     int rebuild_layout();
     int upload_params();
     int launch_prefix(bool profile);   // memsets, hash, scan, sort, density
+    int launch_prefix_args(const StepArgs& a, bool profile);
+    int prefix_scene(const Scene& s);  // the prefix over one scene's tiles
     int launch_suffix(bool profile);   // normals, force + integrator, [XSPH]
     int ensure_prefix();               // the next substep's prefix, computed once
     int materialize(Scene& s);         // apply a pending XSPH update to the state

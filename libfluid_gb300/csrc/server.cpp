@@ -174,10 +174,18 @@ void sph_server::loop() {
             }
             st.peak_live_particles = std::max(st.peak_live_particles, lp);
         }
-        for (Request* r : finished) {
+        // Read every finished scene before removing any: the first read runs
+        // the next substep's prefix (deferred XSPH) and the others reuse it.
+        std::vector<int> got(finished.size());
+        for (size_t fi = 0; fi < finished.size(); ++fi) {
+            Request* r = finished[fi];
             r->out_pos.resize((size_t)r->n * 3);
             r->out_vel.resize((size_t)r->n * 3);
-            const int g = eng->get_state(r->scene, r->out_pos.data(), nullptr, r->out_vel.data(), r->n);
+            got[fi] = eng->get_state(r->scene, r->out_pos.data(), nullptr, r->out_vel.data(), r->n);
+        }
+        for (size_t fi = 0; fi < finished.size(); ++fi) {
+            Request* r = finished[fi];
+            const int g = got[fi];
             eng->remove_scene(r->scene);
             std::lock_guard<std::mutex> lk(mu);
             used_bytes -= r->bytes;
