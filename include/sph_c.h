@@ -112,6 +112,16 @@ int sph_set_gravity(sph_system* s, float gx, float gy, float gz);
 /* Rectangular box [0,lx]x[0,ly]x[0,lz] with cell size h (the smoothing
  * length).  Reallocates the grid; particle state is kept. */
 int sph_set_domain(sph_system* s, float lx, float ly, float lz, float h);
+/* Boundary shape.  The reference's boundarySDF (fluidutil.cu:85-102) returns
+ * the box distance; it also computes, and discards, the distance to the
+ * sphere of radius 0.5 about the cube's centre.  SPH_BOUNDARY_SPHERE uses
+ * that sphere (radius: the box's smallest half extent, about its centre) for
+ * the boundary density, adhesion and the integrator's boundary projection.
+ * The grid still covers the box. */
+#define SPH_BOUNDARY_BOX 0
+#define SPH_BOUNDARY_SPHERE 1
+int sph_set_boundary(sph_system* s, int shape);
+int sph_get_boundary(const sph_system* s, int* shape);
 
 /* Whole parameter set, for inspection and bulk configuration. */
 typedef struct sph_params {
@@ -153,7 +163,7 @@ typedef struct sph_snapshot_header {
     uint32_t n;
     uint32_t header_bytes;   /* 128 */
     sph_params params;
-    uint32_t reserved[6];
+    uint32_t reserved[6];    /* [0]: boundary shape (SPH_BOUNDARY_*); others 0 */
 } sph_snapshot_header;
 uint64_t sph_snapshot_bytes(uint32_t n);
 int sph_snapshot(sph_system* s, void* buf, uint64_t cap, uint64_t* written);
@@ -266,6 +276,7 @@ int sph_batch_step(sph_batch* b, uint32_t substeps);
 int sph_batch_step_async(sph_batch* b, uint32_t substeps);
 int sph_batch_sync(sph_batch* b);
 int sph_batch_get_state(sph_batch* b, int scene_id, float* pos, float* colour, float* vel, uint32_t n);
+int sph_batch_set_boundary(sph_batch* b, int scene_id, int shape);
 /* Snapshot / resume of one scene, in the sph_snapshot format (above). */
 int sph_batch_snapshot(sph_batch* b, int scene_id, void* buf, uint64_t cap, uint64_t* written);
 int sph_batch_restore(sph_batch* b, int scene_id, const void* buf, uint64_t bytes);

@@ -156,6 +156,16 @@ class FluidSystem:
     def setDomain(self, lx: float, ly: float, lz: float, h: float) -> None:
         self._ck(self._L.sph_set_domain(self._h, lx, ly, lz, h))
 
+    def setBoundary(self, shape: int) -> None:
+        """0: the box (the reference's boundary); 1: the sphere of radius the
+        box's smallest half extent about its centre."""
+        self._ck(self._L.sph_set_boundary(self._h, shape))
+
+    def getBoundary(self) -> int:
+        out = C.c_int(0)
+        self._ck(self._L.sph_get_boundary(self._h, C.byref(out)))
+        return out.value
+
     def getParams(self) -> dict:
         p = SphParams()
         self._ck(self._L.sph_get_params(self._h, C.byref(p)))

@@ -91,6 +91,8 @@ SIGNATURES = [
     ("sph_set_mass", _I, [_P, _F]),
     ("sph_set_gravity", _I, [_P, _F, _F, _F]),
     ("sph_set_domain", _I, [_P, _F, _F, _F, _F]),
+    ("sph_set_boundary", _I, [_P, _I]),
+    ("sph_get_boundary", _I, [_P, C.POINTER(_I)]),
     ("sph_get_params", _I, [_P, C.POINTER(SphParams)]),
     ("sph_set_params", _I, [_P, C.POINTER(SphParams)]),
     ("sph_get_derived", _I, [_P, C.POINTER(C.c_double), _I]),

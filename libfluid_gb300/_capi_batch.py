@@ -18,6 +18,7 @@ SIGNATURES = [
     ("sph_batch_add_scene", _I, [_P, C.POINTER(SphParams), _U32, C.POINTER(_I)]),
     ("sph_batch_remove_scene", _I, [_P, _I]),
     ("sph_batch_set_params", _I, [_P, _I, C.POINTER(SphParams)]),
+    ("sph_batch_set_boundary", _I, [_P, _I, _I]),
     ("sph_batch_set_state", _I, [_P, _I, _P, _P, _U32]),
     ("sph_batch_generate_lattice", _I, [_P, _I, C.POINTER(SphLattice), _U32]),
     ("sph_batch_step", _I, [_P, _U32]),

@@ -70,6 +70,8 @@ class Batch:
         p = params_struct(spec)
         self._ck(self._L.sph_batch_add_scene(self._h, C.byref(p), spec.n, C.byref(sid)))
         self.scenes[sid.value] = spec
+        if getattr(spec, "boundary", 0):
+            self._ck(self._L.sph_batch_set_boundary(self._h, sid.value, spec.boundary))
         if generate and getattr(spec, "extra_pos", None) is not None:
             # particles beyond the lattice blocks come from the host (the
             # lattice part is identical to the device generator's)

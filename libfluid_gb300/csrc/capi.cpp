@@ -259,6 +259,7 @@ int sph_snapshot(sph_system* s, void* buf, uint64_t cap, uint64_t* written) {
     sph_get_params(s, &p);
     sph_snapshot_header h;
     sph::snapshot_make_header(h, s->n, p);
+    h.reserved[0] = (uint32_t)s->cfg.boundary;
     std::memcpy(buf, &h, sizeof(h));
     float4* body = reinterpret_cast<float4*>(static_cast<char*>(buf) + sizeof(h));
     int rc = eng_err(s, s->eng->save_state(s->scene, body, s->n));
@@ -273,6 +274,7 @@ int sph_restore(sph_system* s, const void* buf, uint64_t bytes) {
     std::string why;
     if (!sph::snapshot_parse(buf, bytes, &h, &why)) return set_err(s, SPH_EINVAL, why);
     if (h.n != s->n) return set_err(s, SPH_EINVAL, "snapshot particle count differs from the system's");
+    s->cfg.boundary = (int)h.reserved[0];
     int rc = sph_set_params(s, &h.params);
     if (rc) return rc;
     const float4* body = reinterpret_cast<const float4*>(static_cast<const char*>(buf) + sizeof(h));
@@ -346,11 +348,25 @@ int sph_set_params(sph_system* s, const sph_params* o) {
     c.adhesion = o->adhesion; c.vdamp = o->vdamp;
     c.vel_limit = o->vel_limit; c.acc_limit = o->acc_limit; c.dt = o->dt;
     c.gravity[0] = o->gravity[0]; c.gravity[1] = o->gravity[1]; c.gravity[2] = o->gravity[2];
+    c.boundary = s->cfg.boundary;   // not part of sph_params: sph_set_boundary
     DevParams dp;
     std::string e;
     if (!sph::derive_params(c, dp, &e)) return set_err(s, SPH_EINVAL, e);
     s->cfg = c;
     return push_cfg(s);
+}
+
+int sph_set_boundary(sph_system* s, int shape) {
+    if (!s) return SPH_EINVAL;
+    if (shape != SPH_BOUNDARY_BOX && shape != SPH_BOUNDARY_SPHERE)
+        return set_err(s, SPH_EINVAL, "boundary must be SPH_BOUNDARY_BOX or SPH_BOUNDARY_SPHERE");
+    s->cfg.boundary = shape;
+    return push_cfg(s);
+}
+int sph_get_boundary(const sph_system* s, int* shape) {
+    if (!s || !shape) return SPH_EINVAL;
+    *shape = s->cfg.boundary;
+    return SPH_OK;
 }
 
 static int derived_values(const SceneConfig& cfg, double* out, int cap);

@@ -90,6 +90,20 @@ int sph_batch_set_params(sph_batch* b, int scene_id, const sph_params* p) {
     if (!b || !p) return SPH_EINVAL;
     SceneConfig c;
     if (!to_config(p, c, &b->err)) return SPH_EINVAL;
+    if (const sph::Scene* sc = b->eng->scene(scene_id)) c.boundary = sc->cfg.boundary;
+    return berr(b, b->eng->set_config(scene_id, c));
+}
+
+int sph_batch_set_boundary(sph_batch* b, int scene_id, int shape) {
+    if (!b) return SPH_EINVAL;
+    const sph::Scene* sc = b->eng->scene(scene_id);
+    if (!sc) { b->err = "unknown scene id"; return SPH_EINVAL; }
+    if (shape != SPH_BOUNDARY_BOX && shape != SPH_BOUNDARY_SPHERE) {
+        b->err = "boundary must be SPH_BOUNDARY_BOX or SPH_BOUNDARY_SPHERE";
+        return SPH_EINVAL;
+    }
+    SceneConfig c = sc->cfg;
+    c.boundary = shape;
     return berr(b, b->eng->set_config(scene_id, c));
 }
 
@@ -134,6 +148,7 @@ int sph_batch_snapshot(sph_batch* b, int scene_id, void* buf, uint64_t cap, uint
     from_config(sc->cfg, &p);
     sph_snapshot_header h;
     sph::snapshot_make_header(h, sc->n, p);
+    h.reserved[0] = (uint32_t)sc->cfg.boundary;
     std::memcpy(buf, &h, sizeof(h));
     float4* body = reinterpret_cast<float4*>(static_cast<char*>(buf) + sizeof(h));
     int rc = berr(b, b->eng->save_state(scene_id, body, sc->n));
@@ -148,7 +163,9 @@ int sph_batch_restore(sph_batch* b, int scene_id, const void* buf, uint64_t byte
     sph_snapshot_header h;
     if (!sph::snapshot_parse(buf, bytes, &h, &b->err)) return SPH_EINVAL;
     if (h.n != sc->n) { b->err = "snapshot particle count differs from the scene's"; return SPH_EINVAL; }
-    int rc = sph_batch_set_params(b, scene_id, &h.params);
+    int rc = sph_batch_set_boundary(b, scene_id, (int)h.reserved[0]);
+    if (rc) return rc;
+    rc = sph_batch_set_params(b, scene_id, &h.params);
     if (rc) return rc;
     const float4* body = reinterpret_cast<const float4*>(static_cast<const char*>(buf) + sizeof(h));
     return berr(b, b->eng->load_state(scene_id, body, h.n));

@@ -87,6 +87,9 @@ bool derive_params(const SceneConfig& c, DevParams& d, std::string* err) {
     d.grav_x = c.gravity[0]; d.grav_y = c.gravity[1]; d.grav_z = c.gravity[2];
     d.eps = FLT_MIN;
     d.flags = (c.surface_tension != 0.0f) ? 1u : 0u;
+    if (c.boundary != 0 && c.boundary != 1) { if (err) *err = "boundary must be 0 (box) or 1 (sphere)"; return false; }
+    if (c.boundary == 1) d.flags |= SPH_FLAG_SPHERE;
+    d.sphere_r = std::fmin(d.box_bx, std::fmin(d.box_by, d.box_bz));
     const float skin = (c.skin > 0.0f) ? c.skin : SPH_SKIN_DEFAULT;
     const float rs = (1.0f + skin) * h;
     d.skin2 = rs * rs;

@@ -23,6 +23,7 @@ struct SceneConfig {
     float vel_limit = 5.f, acc_limit = 150.f, dt = 0.01f;
     float gravity[3] = {0.f, -9.8f, 0.f};
     float skin = 0.f;                 // neighbour-mask skin in units of h (0: engine default)
+    int boundary = 0;                 // 0: the box; 1: the sphere of radius min half extent about its centre
 };
 
 // Execution choices of the substep.  Defaults are the autotuner's choice

@@ -28,13 +28,25 @@ __device__ __forceinline__ float sdf_box(const DevParams& P, float x, float y, f
     return inner + sqrtf(dot3(px, py, pz, px, py, pz));
 }
 
+// Sphere container: length(p - c) - r (the distance boundarySDF computes but
+// does not return, fluidutil.cu:97-98), c the box centre, r its smallest half
+// extent (0.5 in the unit cube, as there).
+__device__ __forceinline__ float sdf_sphere(const DevParams& P, float x, float y, float z) {
+    const float dx = x - P.box_cx, dy = y - P.box_cy, dz = z - P.box_cz;
+    return sqrtf(dot3(dx, dy, dz, dx, dy, dz)) - P.sphere_r;
+}
+// The scene's boundary distance, negative inside.
+__device__ __forceinline__ float sdf(const DevParams& P, float x, float y, float z) {
+    return (P.flags & SPH_FLAG_SPHERE) ? sdf_sphere(P, x, y, z) : sdf_box(P, x, y, z);
+}
+
 // Central-difference SDF normal (boundaryNormalSDF, fluidutil.cu:104-112),
 // normalised as v * (1/sqrt(v.v)).
 __device__ __forceinline__ float3 sdf_normal(const DevParams& P, float x, float y, float z) {
     const float e = 0.0001f;
-    const float nx = sdf_box(P, x + e, y, z) - sdf_box(P, x - e, y, z);
-    const float ny = sdf_box(P, x, y + e, z) - sdf_box(P, x, y - e, z);
-    const float nz = sdf_box(P, x, y, z + e) - sdf_box(P, x, y, z - e);
+    const float nx = sdf(P, x + e, y, z) - sdf(P, x - e, y, z);
+    const float ny = sdf(P, x, y + e, z) - sdf(P, x, y - e, z);
+    const float nz = sdf(P, x, y, z + e) - sdf(P, x, y, z - e);
     const float inv = 1.0f / sqrtf(dot3(nx, ny, nz, nx, ny, nz));
     return make_float3(nx * inv, ny * inv, nz * inv);
 }

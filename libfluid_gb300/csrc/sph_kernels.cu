@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
             ++j;
         }
     }
-    const float d = fabsf(sdf_box(pp, p.x, p.y, p.z));
+    const float d = fabsf(sdf(pp, p.x, p.y, p.z));
     float corr = sum;
     if (d < pp.h) corr = fmaf(pp.rest_density, 1.0f - boundary_density(pp, d), corr);
     const float rho = (sum == 0.0f) ? pp.rest_density : corr;
@@ -583,7 +583,7 @@ k_force_integrate(const DevParams* __restrict__ params,
         }
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
         ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
-        const float z = -fminf(sdf_box(pp, pi.x, pi.y, pi.z), 0.0f) * 0.25f * pp.inv_particle_size;
+        const float z = -fminf(sdf(pp, pi.x, pi.y, pi.z), 0.0f) * 0.25f * pp.inv_particle_size;
         if (z < 1.0f) {
             const float3 nb = sdf_normal(pp, pi.x, pi.y, pi.z);
             const float denom = 1.0f / powf(1.0f - z, 3.0f);
@@ -619,7 +619,7 @@ k_force_integrate(const DevParams* __restrict__ params,
         const float s = pp.vel_limit / sqrtf(sq);
         vx = vx * s; vy = vy * s; vz = vz * s;
     }
-    const float d = sdf_box(pp, px, py, pz);
+    const float d = sdf(pp, px, py, pz);
     if (d > -pp.particle_size) {
         const float3 nb = sdf_normal(pp, px, py, pz);
         const float s = -(d + pp.particle_size);

@@ -13,6 +13,7 @@
 #define SPH_OKEY_MOVED 0x80000000u  // packed-cell flag: the particle has changed cell since
 #define SPH_OKEY_MAX_DIM 1024u      // grids up to this many cells per axis can defer XSPH
 #define SPH_FLAG_DEFER_XSPH 0x2u    // DevParams.flags: XSPH applied by the next density pass
+#define SPH_FLAG_SPHERE 0x4u        // DevParams.flags: sphere boundary instead of the box
 
 // Derived per-scene parameters (the FluidParamData of fluidparams.cuh:16-69,
 // generalised to a rectangular box [0,L]^3 with cell size h).
@@ -36,11 +37,13 @@ struct DevParams {
     float grav_x, grav_y, grav_z;
     float eps;                    // FLT_MIN (fluidparams.cu:48)
     uint32_t flags;               // bit0: surface tension active (normals pass needed);
-                                  // bit1: the scene defers XSPH (SPH_FLAG_DEFER_XSPH)
+                                  // bit1: the scene defers XSPH (SPH_FLAG_DEFER_XSPH);
+                                  // bit2: sphere boundary (SPH_FLAG_SPHERE)
     float skin2;                  // ((1 + skin) h)^2: radius of the neighbour masks
     float inv_h2;                 // 1/h^2, normalises displacements for the XSPH mask check
     float xsph_disp_limit2;       // (skin/2)^2 * 0.98: largest (displacement/h)^2 XSPH may accept
-    uint32_t pad_[3];
+    float sphere_r;               // sphere boundary (flags bit2): radius about the box centre
+    uint32_t pad_[2];
 };
 
 // Neighbour masks are built with radius (1 + skin) h (default skin below).

@@ -96,6 +96,7 @@ class SceneSpec:
     unit_cube_res: int = 0          # >0: the reference's unit cube with res cells instead of box/h
     extra_pos: np.ndarray | None = None   # host-generated particles after the blocks (e.g. spheres)
     extra_vel: np.ndarray | None = None
+    boundary: int = 0               # 0: the box; 1: the sphere of radius min half extent about its centre
 
     @property
     def n(self) -> int:
@@ -130,6 +131,22 @@ def small_dam_break(seed: int = 1, unit_cube: bool = False) -> SceneSpec:
     if unit_cube:
         s.box, s.unit_cube_res, s.gravity = (1.0, 1.0, 1.0), 50, (0.0, -9.8, 0.0)
     return s
+
+
+def sphere_tank(seed: int = 1) -> SceneSpec:
+    """The sphere boundary: lattice sites (spacing 0.01 m, jittered) inside a
+    sphere of radius 0.34 m about (0.35, 0.35, 0.35), below its centre, in a
+    0.7 m cube whose boundary is the inscribed sphere (radius 0.35 m, so the
+    outer particles feel the wall); h = 0.02 m, dt = 2e-4 s.  About 82,000
+    particles."""
+    sites = sphere_sites((0.35, 0.35, 0.35), 0.34, 0.01)
+    sites = sites[sites[:, 1] <= 0.35]
+    ctr = np.arange(3 * sites.shape[0], dtype=np.uint64).reshape(-1, 3)
+    jit = ((np.float32(2.0) * uniform01(int(np.uint64(seed) * np.uint64(2654435761)), ctr) - np.float32(1.0)) *
+           np.float32(0.05 * 0.01)).astype(np.float32)
+    pos = (sites + jit).astype(np.float32)
+    return SceneSpec(box=(0.7, 0.7, 0.7), h=0.02, blocks=[], mass=1e-3, particle_size=0.005, dt=2e-4, steps=200,
+                     extra_pos=pos, extra_vel=np.zeros_like(pos), boundary=1)
 
 
 def dam_break_1m(seed: int = 1, unit_cube: bool = False) -> SceneSpec:

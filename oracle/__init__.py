@@ -35,6 +35,7 @@ def lib() -> C.CDLL:
         sig = {
             "orc_create": (P, [C.c_int]), "orc_destroy": (None, [P]), "orc_precision": (C.c_int, [P]),
             "orc_init": (C.c_int, [P, U, U]), "orc_set_domain": (C.c_int, [P, F, F, F, F]),
+            "orc_set_boundary": (C.c_int, [P, C.c_int]),
             "orc_set_param": (C.c_int, [P, C.c_int, F]), "orc_set_limits": (C.c_int, [P, F, F]),
             "orc_set_gravity": (C.c_int, [P, F, F, F]),
             "orc_create_block": (C.c_int, [P, U, U, F, F, F, F, F, F]),
@@ -83,6 +84,11 @@ class Oracle:
 
     def set_domain(self, lx, ly, lz, h):
         self._ck(self._L.orc_set_domain(self._h, lx, ly, lz, h))
+
+    def set_boundary(self, shape: int):
+        """0: the box (the reference's boundary); 1: the sphere of radius min
+        half extent about the box centre."""
+        self._ck(self._L.orc_set_boundary(self._h, shape))
 
     def set_param(self, name: str, v: float):
         self._ck(self._L.orc_set_param(self._h, PARAMS[name], v))

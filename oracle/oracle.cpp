@@ -97,6 +97,10 @@ template <class T> struct Params {
     uint32_t res = 0, gx = 1, gy = 1, gz = 1, numCells = 1;
     T inv_cell = T(1);                 // cell scale: grid = floor(p * inv_cell)
     V3<T> box_c{T(0.5), T(0.5), T(0.5)}, box_b{T(0.5), T(0.5), T(0.5)};
+    // boundary shape: 0 the box (the reference's boundarySDF), 1 the sphere of
+    // radius min(box_b) about box_c that boundarySDF computes but does not
+    // return (fluidutil.cu:97-99)
+    int boundary = 0;
     uint32_t numParticles = 0;
     T restDensity{}, invRestDensity{}, gasConstant{}, gamma{}, invGamma{};
     T mass{}, mass2{}, invMass{}, particleSize{}, invParticleSize{};
@@ -253,15 +257,25 @@ template <class T> inline T sdf_box(const Params<T>& P, V3<T> pos) {
     const V3<T> qp = mk(std::fmax(q.x, T(0)), std::fmax(q.y, T(0)), std::fmax(q.z, T(0)));
     return inner + sqrt_(dot(qp, qp));
 }
+// the sphere container: length(p - c) - r (fluidutil.cu:97-98), r the box's
+// smallest half extent (0.5 in the unit cube, as there)
+template <class T> inline T sdf_sphere(const Params<T>& P, V3<T> pos) {
+    const V3<T> d = mk(pos.x - P.box_c.x, pos.y - P.box_c.y, pos.z - P.box_c.z);
+    const T r = std::fmin(P.box_b.x, std::fmin(P.box_b.y, P.box_b.z));
+    return sqrt_(dot(d, d)) - r;
+}
+template <class T> inline T sdf(const Params<T>& P, V3<T> pos) {
+    return P.boundary == 1 ? sdf_sphere(P, pos) : sdf_box(P, pos);
+}
 template <class T> inline V3<T> normalize_(V3<T> v) {
     const T inv = T(1) / sqrt_(dot(v, v));
     return v * inv;
 }
 template <class T> inline V3<T> sdf_normal(const Params<T>& P, V3<T> p) {
     const T e = T(0.0001f);
-    return normalize_(mk(sdf_box(P, mk(p.x + e, p.y, p.z)) - sdf_box(P, mk(p.x - e, p.y, p.z)),
-                         sdf_box(P, mk(p.x, p.y + e, p.z)) - sdf_box(P, mk(p.x, p.y - e, p.z)),
-                         sdf_box(P, mk(p.x, p.y, p.z + e)) - sdf_box(P, mk(p.x, p.y, p.z - e))));
+    return normalize_(mk(sdf(P, mk(p.x + e, p.y, p.z)) - sdf(P, mk(p.x - e, p.y, p.z)),
+                         sdf(P, mk(p.x, p.y + e, p.z)) - sdf(P, mk(p.x, p.y - e, p.z)),
+                         sdf(P, mk(p.x, p.y, p.z + e)) - sdf(P, mk(p.x, p.y, p.z - e))));
 }
 
 // ---- spatial hash: hash.cu:10-27, fluidutil.cu:15-39 ----
@@ -391,7 +405,7 @@ template <class T> struct Sim : SimBase {
                 const T rr = dot(d, d);
                 if (o != i && rr <= P.h2) { sum = fma_(P.mass, poly6(P, sqrt_(rr)), sum); cnt++; }
             });
-            const T d = std::fabs(sdf_box(P, pi));
+            const T d = std::fabs(sdf(P, pi));
             T corr = sum;
             if (d < P.h) corr = fma_(P.restDensity, T(1.0f) - boundary_density(P, d), corr);
             rho_sum[i] = sum;
@@ -464,7 +478,7 @@ template <class T> struct Sim : SimBase {
             fv[i] = P.viscosity * vs;
             ft[i] = P.surfaceTension * ts;
             fa[i] = mk(T(0), T(0), T(0));
-            const T z = -std::fmin(sdf_box(P, pi), T(0)) * T(0.25f) * P.invParticleSize;
+            const T z = -std::fmin(sdf(P, pi), T(0)) * T(0.25f) * P.invParticleSize;
             if (z < T(1)) {
                 const V3<T> nb = sdf_normal(P, pi);
                 const T denom = T(1.0f) / pow_(T(1) - z, T(3));
@@ -495,7 +509,7 @@ template <class T> struct Sim : SimBase {
             v = fmaV(hs, P.dt, v);
             sq = dot(v, v);
             if (sq > P.velLimit2) v = v * (P.velLimit / sqrt_(sq));
-            const T d = sdf_box(P, p);
+            const T d = sdf(P, p);
             if (d > -P.particleSize) {
                 const V3<T> nb = sdf_normal(P, p);
                 p = fmaV(-(d + P.particleSize), nb, p);
@@ -603,6 +617,13 @@ int orc_init(void* s, uint32_t n, uint32_t res) { DISPATCH(s, S.init(n, res)); r
 int orc_set_domain(void* s, float lx, float ly, float lz, float h) {
     if (!(h > 0.0f) || !(lx > 0.0f) || !(ly > 0.0f) || !(lz > 0.0f)) return 1;
     DISPATCH(s, { set_domain(S.P, lx, ly, lz, h); S.resize_cells(); });
+    return 0;
+}
+// Boundary shape (0 box, 1 sphere); no reference setter: the reference
+// always returns the box distance.
+int orc_set_boundary(void* s, int shape) {
+    if (shape != 0 && shape != 1) return 1;
+    DISPATCH(s, S.P.boundary = shape);
     return 0;
 }
 int orc_set_param(void* s, int which, float v) {

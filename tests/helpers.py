@@ -13,6 +13,8 @@ def configure_oracle(o: "oracle.Oracle", spec: W.SceneSpec, pos=None, vel=None):
     o.init(n, spec.unit_cube_res or 1)
     if not spec.unit_cube_res:
         o.set_domain(*spec.box, spec.h)
+    if spec.boundary:
+        o.set_boundary(spec.boundary)
     for k, v in spec.params().items():
         if k == "gravity":
             o.set_gravity(*v)
@@ -30,6 +32,8 @@ def configure_gpu(fs, spec: W.SceneSpec, pos=None, vel=None):
     fs.init(n, spec.unit_cube_res or 1)
     if not spec.unit_cube_res:
         fs.setDomain(*spec.box, spec.h)
+    if spec.boundary:
+        fs.setBoundary(spec.boundary)
     p = spec.params()
     fs.setParams(rest_density=p["rest_density"], mass=p["mass"], gamma=p["gamma"],
                  gas_constant=p["gas_constant"], viscosity=p["viscosity"], xsph=p["xsph"],

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+from helpers import configure_oracle
 from libfluid_gb300 import _capi, workloads as W
 from libfluid_gb300.batch import params_struct
 
@@ -188,3 +189,24 @@ def test_batch_manifest_shapes():
 
 
 _LATTICE_SHA256 = "b48b96bbb22a8c30a10ad69c042322382acbb27e722672b682def8a1479bce9c"
+
+
+def test_sphere_boundary_oracle():
+    """The sphere boundary (the distance boundarySDF computes but discards):
+    particles start inside the sphere and stay inside it; with the box
+    boundary the same start differs."""
+    spec = W.sphere_tank(seed=3)
+    o = configure_oracle(oracle.Oracle(32), spec)
+    for _ in range(3):
+        o.advance(spec.dt, 1)
+    pos = o.get("pos").astype(np.float64)
+    r = np.linalg.norm(pos - 0.35, axis=1)
+    assert np.all(np.isfinite(pos))
+    assert r.max() <= 0.35 - 0.9 * spec.particle_size + 1e-6
+    spec_box = W.sphere_tank(seed=3)
+    spec_box.boundary = 0
+    ob = configure_oracle(oracle.Oracle(32), spec_box)
+    ob.advance(spec.dt, 1)
+    o1 = configure_oracle(oracle.Oracle(32), spec)
+    o1.advance(spec.dt, 1)
+    assert not np.array_equal(o1.get("density"), ob.get("density"))

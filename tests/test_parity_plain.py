@@ -108,3 +108,15 @@ def test_unit_cube_variant_first_steps():
     assert rel_err(fs.debug("density"), o32.get("density"), 1.0) < RTOL_DENSITY
     pos, _, _ = fs.exportToData()
     assert rel_err(pos, o32.get("pos"), 1e-3) < 1e-5
+
+
+def test_sphere_boundary_matches_oracle():
+    """The sphere boundary on the GPU against the oracle after one substep:
+    densities (with the boundary term) and positions (with the projection)."""
+    spec = W.sphere_tank(seed=4)
+    fs, o32, _ = _run_one(spec)
+    assert fs.getBoundary() == 1
+    assert rel_err(fs.debug("density"), o32.get("density"), 1.0) < RTOL_DENSITY
+    pos, _, _ = fs.exportToData()
+    assert rel_err(pos, o32.get("pos"), 1e-3) < RTOL_POS
+    fs.close()
