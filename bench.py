@@ -333,7 +333,12 @@ def run_ours(args, dist):
         spec.unit_cube_res ** 3
     kern = {k: v for k, v in per_launch.items() if k not in ("substep",) and v > 0}
     dom = max(kern, key=kern.get)
-    alg = ALG_BYTES.get(dom, 0) * n + (CELL_BYTES * cells if dom == "scan" else 0)
+    alg_bytes = dict(ALG_BYTES)
+    if per_launch.get("xsph", 0.0) < 0.05 * per_launch.get("density", 1.0):
+        # deferred XSPH: the update runs inside the density pass (its reads and
+        # writes: P, V, rho 28 B, V 12 B) and there is no XSPH pass
+        alg_bytes["density"] += alg_bytes["xsph"]
+    alg = alg_bytes.get(dom, 0) * n + (CELL_BYTES * cells if dom == "scan" else 0)
     peaks = measured_peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     achieved = alg / (per_launch[dom] * 1e-3) / 1e9
