@@ -234,11 +234,21 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 }
 
 // ---------------------------------------------------------------------------
-// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84).  WALK selects
-// one loop flattened across the rows (0) or one candidate loop per (y,z) row
-// with two loads in flight (1); the candidates and their order are the same.
-// (A flattened loop over a row table in shared memory measured slower here:
-// 64 registers against 48.)
+// Density + Tait EOS (computeDensity, fluidphysics.cu:8-84), in two phases.
+//
+// Phase 1 scans every candidate of the 27 cells with the distance test alone
+// and records, per (y,z) row, a bit per candidate within h (density pairs),
+// within eps (coincident) and, with SKIN, within the skin radius.  The words
+// go to the neighbour masks of the later passes (rows 0-8 the skin words,
+// rows 9-17 the exact neighbours eps < r^2 <= h^2, j != i) and to a row table
+// in shared memory (build_row_table's layout).  Phase 2 walks that table and
+// does the kernel arithmetic for the density pairs only (about one candidate
+// in six), so a warp no longer runs the neighbour path on every candidate
+// that any of its lanes accepts.  Rows longer than 32 candidates are walked
+// in full in phase 2 with the test repeated.  Both phases visit candidates in
+// the reference's order, so the sum is the candidate-order sum.  WALK selects
+// phase 1's loop: flattened across the rows (0) or one loop per row with two
+// loads in flight (1); the words are the same.
 //
 // Deferred XSPH.  For a scene whose previous substep ended without its XSPH
 // update (pend[scene] != 0), P1 holds that substep's post-integration
@@ -247,10 +257,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // (correctVelocityXSPH, fluidphysics.cu:355-409) sums over pairs with
 // r^2 <= h^2 at these positions whose previous cells are adjacent (its cell
 // lists were those of the previous sort); every such pair is within h now, so
-// this candidate walk meets all of them, and the previous-cell test keeps
-// exactly the reference's pairs.  The poly6 weight is the one the density sum
-// just computed.  The corrected velocity goes to Vc, which the force pass
-// reads; without a pending update Vc = V1.
+// phase 2 meets all of them, and the previous-cell test keeps exactly the
+// reference's pairs.  The poly6 weight is the one the density sum uses.  The
+// corrected velocity goes to Vc, which the force pass reads; without a
+// pending update Vc = V1.
 // ---------------------------------------------------------------------------
 #ifndef DENSITY_MINB
 #define DENSITY_MINB 4
@@ -267,6 +277,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                                                       const uint32_t* __restrict__ pend, float4* __restrict__ Vc,
                                                       uint32_t* __restrict__ nbr_out, uint32_t ntiles,
                                                       uint32_t* __restrict__ tile_ctr) {
+  extern __shared__ uint32_t s_rows[];
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
@@ -282,105 +293,106 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         return;
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
-    // the skin-radius masks serve only the per-substep XSPH pass
-    const float h2 = pp.h2, h = pp.h, mass = pp.mass, c6 = pp.poly6, skin2 = SKIN ? pp.skin2 : pp.h2, eps = pp.eps;
+    // the skin-radius words serve only the per-substep XSPH pass
+    const float h2 = pp.h2, skin2 = SKIN ? pp.skin2 : pp.h2, eps = pp.eps;
+    uint32_t* tab = s_rows + threadIdx.x;
+    const uint32_t ts = blockDim.x;
+    uint32_t live = 0u, full = 0u;
+
+    // ---- phase 1: distance test of every candidate ----
+    auto visit = [&](const float4& q, uint32_t bit, uint32_t& dm, uint32_t& ez, uint32_t& sm) {
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        const float rr = dot3(dx, dy, dz, dx, dy, dz);
+        if (rr <= h2) dm |= bit;
+        if (rr <= eps) ez |= bit;
+        if (SKIN && rr <= skin2) sm |= bit;
+    };
+    // A row's words (bit b = candidate jb0 + b, b < 32) minus the particle
+    // itself, stored to the masks and the row table.
+    auto close_row = [&](int r, uint32_t jb0, uint32_t je0, uint32_t dm, uint32_t ez, uint32_t sm) {
+        const uint32_t so = k - jb0;
+        const uint32_t notself = (so < 32u) ? ~(1u << so) : ~0u;
+        dm &= notself;
+        if (SKIN) mask[(size_t)r * mask_stride + k] = sm & notself;
+        mask[(size_t)(9 + r) * mask_stride + k] = dm & ~ez;
+        const uint32_t len = je0 - jb0;
+        const bool f = len > 32u;
+        const uint32_t v = f ? len : dm;
+        tab[r * ts] = jb0;
+        tab[(9 + r) * ts] = v;
+        if (f) full |= 1u << r;
+        if (v) live |= 1u << r;
+    };
+    if (WALK == 1) {
+#pragma unroll 1
+        for (int r = 0; r < 9; ++r) {
+            uint32_t jb0, je0;
+            if (!row_range(pp, start, sc.cell_base, delta, g, r, jb0, je0)) continue;
+            uint32_t dm = 0u, ez = 0u, sm = 0u, bit = 1u;
+            uint32_t jj = jb0;
+            for (; jj + 2u <= je0; jj += 2u) {
+                const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
+                visit(q0, bit, dm, ez, sm);
+                visit(q1, bit << 1, dm, ez, sm);
+                bit <<= 2;
+            }
+            if (jj < je0) visit(__ldg(P1 + jj), bit, dm, ez, sm);
+            close_row(r, jb0, je0, dm, ez, sm);
+        }
+    } else {
+        // one loop across all 9 rows, so lanes do not wait at row ends
+        int r = -1;
+        uint32_t jb = 0, j = 0, je = 0, dm = 0u, ez = 0u, sm = 0u, bit = 0u;
+        bool valid = false;
+        for (;;) {
+            if (j >= je) {
+                if (valid) close_row(r, jb, je, dm, ez, sm);
+                if (++r >= 9) break;
+                dm = ez = sm = 0u;
+                bit = 1u;
+                valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
+                if (!valid) jb = je = 0;
+                j = jb;
+                continue;
+            }
+            visit(__ldg(P1 + j), bit, dm, ez, sm);
+            bit <<= 1;
+            ++j;
+        }
+    }
+
+    // ---- phase 2: the density pairs, in candidate order ----
+    const float h = pp.h, mass = pp.mass, c6 = pp.poly6;
     float sum = 0.0f;
     uint32_t cnt = 0;
     // deferred XSPH of the previous substep (only for particles that had a cell then)
     const uint32_t oi = (__ldg(pend + t.x) != 0u) ? __ldg(okey1 + k) : SPH_OKEY_NULL;
     const bool xs = oi != SPH_OKEY_NULL;
     float ax = 0.f, ay = 0.f, az = 0.f;
-    // One XSPH pair term of the pending update, given the pair's poly6 weight.
-    auto xsph_term = [&](const float4& q, const float4& vj, uint32_t oj, float w) {
-        const float rs = p.w + q.w;   // the previous substep's densities
-        if (rs > eps && cells_adjacent_fast(oi, oj)) {
-            const float coeff = w * __fdividef(pp.two_mass, rs);
-            ax = fmaf(coeff, vj.x - vi.x, ax);
-            ay = fmaf(coeff, vj.y - vi.y, ay);
-            az = fmaf(coeff, vj.z - vi.z, az);
-        }
-    };
-    // The pending update's pairs of one row, right after the row's candidate
-    // scan (their positions are still in L1): the neighbours just recorded
-    // (eps < r^2 <= h^2, offsets below 32), each pair's loads issued together.
-    // The few pairs the row word cannot hold are taken inline in the scan.
-    auto xsph_row = [&](uint32_t jb0, uint32_t be0) {
-        while (be0) {
-            const int b = __ffs(be0) - 1;
-            be0 &= be0 - 1u;
-            const uint32_t j = jb0 + (uint32_t)b;
-            const float4 q = __ldg(P1 + j), vj = __ldg(V1 + j);
-            const uint32_t oj = __ldg(okey1 + j);
-            const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-            const float rr = dot3(dx, dy, dz, dx, dy, dz);
+    TableWalk walk(tab, ts, live, full);
+    uint32_t j;
+    while (walk.next(j)) {
+        const float4 q = __ldg(P1 + j);
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        const float rr = dot3(dx, dy, dz, dx, dy, dz);
+        // true for every recorded bit; the test matters in rows walked in full
+        if (rr <= h2 && j != k) {
             const float rd = sqrtf(rr);
             const float x = fmaf(-rd, rd, h2);
             const float w = (rd >= h) ? 0.0f : c6 * (x * x * x);
-            xsph_term(q, vj, oj, w);
-        }
-    };
-    // Every candidate is tested here and recorded per row for the later
-    // passes: mask words 0-8 hold the candidates within the skin radius
-    // (XSPH), words 9-17 the exact neighbours j != i, eps < r^2 <= h^2 (the
-    // normal and force passes' test, evaluated bit for bit the same way).
-    auto visit = [&](const float4& q, uint32_t jj, uint32_t jb0, uint32_t& bs0, uint32_t& be0) {
-        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
-        const float rr = dot3(dx, dy, dz, dx, dy, dz);
-        if (rr <= skin2 && jj != k) {
-            const uint32_t off = jj - jb0;
-            const uint32_t bit = (off < 32u) ? (1u << off) : 0u;
-            bs0 |= bit;
-            if (rr <= h2) {
-                if (rr > eps) be0 |= bit;
-                const float rd = sqrtf(rr);
-                const float x = fmaf(-rd, rd, h2);
-                const float w = (rd >= h) ? 0.0f : c6 * (x * x * x);
-                sum = fmaf(mass, w, sum);
-                cnt++;
-                // XSPH pairs outside the row word: coincident particles and
-                // offsets of 32 and beyond
-                if (xs && (rr <= eps || off >= 32u)) xsph_term(q, __ldg(V1 + jj), __ldg(okey1 + jj), w);
-            }
-        }
-    };
-    if (WALK == 1) {
-#pragma unroll 1
-        for (int rr = 0; rr < 9; ++rr) {
-            uint32_t jb0, je0, bs0 = 0u, be0 = 0u;
-            if (row_range(pp, start, sc.cell_base, delta, g, rr, jb0, je0)) {
-                uint32_t jj = jb0;
-                for (; jj + 2u <= je0; jj += 2u) {
-                    const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
-                    visit(q0, jj, jb0, bs0, be0);
-                    visit(q1, jj + 1u, jb0, bs0, be0);
+            sum = fmaf(mass, w, sum);
+            cnt++;
+            if (xs) {
+                const float4 vj = __ldg(V1 + j);
+                const uint32_t oj = __ldg(okey1 + j);
+                const float rs = p.w + q.w;   // the previous substep's densities
+                if (rs > eps && cells_adjacent_fast(oi, oj)) {
+                    const float coeff = w * __fdividef(pp.two_mass, rs);
+                    ax = fmaf(coeff, vj.x - vi.x, ax);
+                    ay = fmaf(coeff, vj.y - vi.y, ay);
+                    az = fmaf(coeff, vj.z - vi.z, az);
                 }
-                if (jj < je0) visit(__ldg(P1 + jj), jj, jb0, bs0, be0);
-                if (SKIN) mask[(size_t)rr * mask_stride + k] = bs0;
-                mask[(size_t)(9 + rr) * mask_stride + k] = be0;
-                if (xs) xsph_row(jb0, be0);
             }
-        }
-    } else {
-        // one loop across all 9 rows, so lanes do not wait at row ends
-        int r = -1;
-        uint32_t jb = 0, j = 0, je = 0, bs = 0u, be = 0u;
-        bool valid = false;
-        for (;;) {
-            if (j >= je) {
-                if (valid) {
-                    if (SKIN) mask[(size_t)r * mask_stride + k] = bs;
-                    mask[(size_t)(9 + r) * mask_stride + k] = be;
-                    if (xs) xsph_row(jb, be);
-                }
-                if (++r >= 9) break;
-                bs = be = 0u;
-                valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
-                if (!valid) jb = je = 0;
-                j = jb;
-                continue;
-            }
-            visit(__ldg(P1 + j), j, jb, bs, be);
-            ++j;
         }
     }
     const float d = fabsf(sdf(pp, p.x, p.y, p.z));
@@ -846,7 +858,9 @@ cudaError_t init_kernel_attributes() {
     const void* fns[] = {
         (const void*)k_force_integrate<true, 3, true>, (const void*)k_force_integrate<true, 4, true>,
         (const void*)k_force_integrate<false, 3, true>, (const void*)k_force_integrate<false, 4, true>,
-        (const void*)k_normals<true>};
+        (const void*)k_normals<true>,
+        (const void*)k_density<0, false>, (const void*)k_density<0, true>,
+        (const void*)k_density<1, false>, (const void*)k_density<1, true>};
     for (const void* f : fns) {
         const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
         if (e != cudaSuccess) return e;
@@ -882,8 +896,9 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
     const bool rows = (a.variant & SPH_VARIANT_DENSITY_ROWS) != 0u;
     auto kern = a.skin_masks ? (rows ? k_density<1, true> : k_density<0, true>)
                              : (rows ? k_density<1, false> : k_density<0, false>);
-    kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
-                                         a.V1, a.okey1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
+    const size_t smem = (size_t)18 * a.block * sizeof(uint32_t);   // the row table
+    kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
+                                            a.V1, a.okey1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
 }
 cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,
