@@ -298,6 +298,8 @@ def run_ours(args, dist):
     fs = FluidSystem(dist.local)
     configure(fs, spec, pos, vel)
     L = _capi.lib()
+    if args.variant is not None:
+        fs.setExec(variant=args.variant)
 
     # ---- warm-up ----
     for _ in range(args.warmup):
@@ -570,6 +572,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-refcuda", action="store_true")
+    ap.add_argument("--variant", type=int, default=None,
+                    help="plain workload: kernel variant bits (SPH_VARIANT_*; default: the compiled default)")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="served workload: number of requests")
     # the knee is near 55 req/s (mean request 1.25e7 particle-steps, ~7e8 particle-steps/s

@@ -98,7 +98,7 @@ bool derive_params(const SceneConfig& c, DevParams& d, std::string* err) {
     return true;
 }
 
-uint64_t Engine::bytes_per_particle() { return 10 * 16 + 6 * 4 + 18 * 4; }
+uint64_t Engine::bytes_per_particle() { return 10 * 16 + 6 * 4 + SPH_MASK_ROWS * 4; }
 uint64_t Engine::bytes_per_cell() { return 2 * 4 + 1; }
 const char* Engine::pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : "?"; }
 
@@ -218,7 +218,7 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
         if (mask_) cudaFree(mask_);
         mask_ = nullptr;
         {
-            cudaError_t e = cudaMalloc((void**)&mask_, 18 * np * sizeof(uint32_t));
+            cudaError_t e = cudaMalloc((void**)&mask_, (size_t)SPH_MASK_ROWS * np * sizeof(uint32_t));
             if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
         }
         if (dbg_nbr_) { cudaFree(dbg_nbr_); dbg_nbr_ = nullptr; }

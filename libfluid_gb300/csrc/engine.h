@@ -167,7 +167,7 @@ private:
     uint32_t *pend_ = nullptr;                      // per scene-table entry: XSPH update pending
     uint32_t *key_ = nullptr, *slot_ = nullptr, *tmp_ = nullptr, *perm_ = nullptr;
     uint32_t *count_ = nullptr, *start_ = nullptr, *scan_sums_ = nullptr, *status_ = nullptr;
-    uint32_t *mask_ = nullptr;        // 9 neighbour-mask words per slot
+    uint32_t *mask_ = nullptr;        // SPH_MASK_ROWS neighbour-mask words per slot
     uint32_t *scal_ = nullptr;        // per-substep scalars: [0] displacement max, [4..7] tile counters
     ExecConfig exec_;
     int sm_count_ = 1;

@@ -189,7 +189,7 @@ __device__ __forceinline__ void for_masked(const DevParams& P, const uint32_t* _
     }
 }
 
-// Candidate walk over one of a particle's mask sets, flattened across the 9
+// Candidate walk over a particle's skin words, flattened across the 9
 // rows: next() yields the next recorded candidate, moving to the next row
 // inside the same call, so lanes of a warp never wait for each other at row
 // boundaries.  Rows longer than 32 candidates carry no mask and yield every
@@ -229,13 +229,60 @@ struct MaskWalk {
     }
 };
 
+// Walk of the exact-neighbour words of a particle's rows, flattened across
+// the 9 rows and their halves.
+struct WideMaskWalk {
+    const DevParams& P;
+    const uint32_t* __restrict__ start;
+    uint32_t cell_base, delta;
+    int3 g;
+    const uint32_t* __restrict__ mask;   // exact rows (SPH_MASK_EXACT)
+    size_t stride;
+    uint32_t k;
+    int r;
+    uint32_t jb, je, j, bits, len;
+    bool full, second;
+    __device__ __forceinline__ WideMaskWalk(const DevParams& P_, const uint32_t* __restrict__ start_, uint32_t cb,
+                                            uint32_t delta_, int3 g_, const uint32_t* __restrict__ mask_,
+                                            size_t stride_, uint32_t k_)
+        : P(P_), start(start_), cell_base(cb), delta(delta_), g(g_), mask(mask_), stride(stride_), k(k_), r(-1),
+          jb(0), je(0), j(0), bits(0), len(0), full(false), second(false) {}
+    __device__ __forceinline__ bool next(uint32_t& cand) {
+        for (;;) {
+            if (full) {
+                if (j < je) { cand = j++; return true; }
+                full = false;
+            } else if (bits) {
+                const int b = __ffs(bits) - 1;
+                bits &= bits - 1u;
+                cand = jb + (uint32_t)b;
+                return true;
+            }
+            if (!second && r >= 0 && len > 32u && len <= SPH_WIDE_ROW) {
+                second = true;
+                jb += 32u;
+                bits = __ldg(mask + (size_t)(2 * r + 1) * stride + k);
+                continue;
+            }
+            if (++r >= 9) return false;
+            second = false;
+            if (!row_range(P, start, cell_base, delta, g, r, jb, je)) { len = 0; continue; }
+            len = je - jb;
+            if (len > SPH_WIDE_ROW) { full = true; j = jb; }
+            else bits = __ldg(mask + (size_t)(2 * r) * stride + k);
+        }
+    }
+};
+
 // Row table of one particle's neighbourhood, kept in the block's shared
 // memory (a column per thread: entry e of thread t at tab[e*ts + t]):
-// entries 0-8 the first slot jb of each row, 9-17 the row's mask word (or,
-// for a row longer than 32 candidates, its length).  `live` has a bit per
-// row with something to visit, `full` per row walked in full.  All 27 loads
-// are independent, so they are issued together, and TableWalk below moves
-// between rows with two shared-memory reads instead of dependent global loads.
+// entries 0-8 the first slot jb of each row, 9-26 the rows' exact-neighbour
+// words (entry 9 + 2r + h), or, for a row longer than 64 candidates, its
+// length in entry 9 + 2r.  `live` has a bit per half-row (2r + h) with
+// something to visit, `full` one (2r) per row walked in full.  The row
+// starts and first words are loaded together; second words only for rows
+// longer than 32.  TableWalk below moves between rows with two
+// shared-memory reads instead of dependent global loads.
 __device__ __forceinline__ void build_row_table(const DevParams& P, const uint32_t* __restrict__ start,
                                                 uint32_t cell_base, uint32_t delta, int3 g,
                                                 const uint32_t* __restrict__ mask, size_t stride, uint32_t k,
@@ -245,20 +292,26 @@ __device__ __forceinline__ void build_row_table(const DevParams& P, const uint32
 #pragma unroll
     for (int r = 0; r < 9; ++r) {
         uint32_t jb, je;
-        const uint32_t w = __ldg(mask + (size_t)r * stride + k);
+        const uint32_t w0 = __ldg(mask + (size_t)(2 * r) * stride + k);
         if (!row_range(P, start, cell_base, delta, g, r, jb, je)) continue;
         const uint32_t len = je - jb;
-        const bool f = len > 32u;
-        const uint32_t v = f ? len : w;
-        if (f) full |= 1u << r;
-        if (v) live |= 1u << r;
         tab[r * ts] = jb;
-        tab[(9 + r) * ts] = v;
+        if (len > SPH_WIDE_ROW) {
+            full |= 1u << (2 * r);
+            live |= 1u << (2 * r);
+            tab[(9 + 2 * r) * ts] = len;
+        } else {
+            const uint32_t w1 = (len > 32u) ? __ldg(mask + (size_t)(2 * r + 1) * stride + k) : 0u;
+            tab[(9 + 2 * r) * ts] = w0;
+            tab[(10 + 2 * r) * ts] = w1;
+            if (w0) live |= 1u << (2 * r);
+            if (w1) live |= 1u << (2 * r + 1);
+        }
     }
 }
 
-// Walk of a row table in MaskWalk's order (rows ascending, candidates of a row
-// ascending).
+// Walk of a row table in WideMaskWalk's order (rows ascending, candidates of
+// a row ascending).
 struct TableWalk {
     const uint32_t* tab;
     uint32_t ts, live, full, jb, bits, j, je;
@@ -274,11 +327,11 @@ struct TableWalk {
             }
             if (j < je) { cand = j++; return true; }
             if (!live) return false;
-            const int r = __ffs(live) - 1;
+            const int e = __ffs(live) - 1;
             live &= live - 1u;
-            jb = tab[r * ts];
-            const uint32_t w = tab[(9 + r) * ts];
-            if ((full >> r) & 1u) { j = jb; je = jb + w; }
+            jb = tab[(e >> 1) * ts] + ((uint32_t)(e & 1) << 5);
+            const uint32_t w = tab[(9 + e) * ts];
+            if ((full >> e) & 1u) { j = jb; je = jb + w; }
             else bits = w;
         }
     }

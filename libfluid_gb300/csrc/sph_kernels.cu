@@ -236,19 +236,21 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // ---------------------------------------------------------------------------
 // Density + Tait EOS (computeDensity, fluidphysics.cu:8-84), in two phases.
 //
-// Phase 1 scans every candidate of the 27 cells with the distance test alone
-// and records, per (y,z) row, a bit per candidate within h (density pairs),
-// within eps (coincident) and, with SKIN, within the skin radius.  The words
-// go to the neighbour masks of the later passes (rows 0-8 the skin words,
-// rows 9-17 the exact neighbours eps < r^2 <= h^2, j != i) and to a row table
-// in shared memory (build_row_table's layout).  Phase 2 walks that table and
+// Phase 1 scans the candidates of the 27 cells, 32 at a time, with the
+// distance test alone and records a bit per candidate within h (density
+// pairs), within eps (coincident) and, with SKIN, within the skin radius.  The
+// words go to the neighbour masks of the later passes (SPH_MASK_SKIN rows for
+// rows of up to 32 candidates; SPH_MASK_EXACT rows, two words per row of up to
+// 64: the exact neighbours eps < r^2 <= h^2, j != i) and to a row table in
+// shared memory (build_row_table's layout).  Phase 2 walks that table and
 // does the kernel arithmetic for the density pairs only (about one candidate
 // in six), so a warp no longer runs the neighbour path on every candidate
-// that any of its lanes accepts.  Rows longer than 32 candidates are walked
-// in full in phase 2 with the test repeated.  Both phases visit candidates in
-// the reference's order, so the sum is the candidate-order sum.  WALK selects
-// phase 1's loop: flattened across the rows (0) or one loop per row with two
-// loads in flight (1); the words are the same.
+// that any of its lanes accepts.  Rows longer than 64 candidates are not
+// scanned in phase 1; phase 2 walks them in full with the test.  Both phases
+// visit candidates in the reference's order, so the sum is the
+// candidate-order sum.  WALK selects phase 1's loop: flattened across the
+// rows (0) or one loop per row with two loads in flight (1); the words are
+// the same.
 //
 // Deferred XSPH.  For a scene whose previous substep ended without its XSPH
 // update (pend[scene] != 0), P1 holds that substep's post-integration
@@ -307,52 +309,82 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         if (rr <= eps) ez |= bit;
         if (SKIN && rr <= skin2) sm |= bit;
     };
-    // A row's words (bit b = candidate jb0 + b, b < 32) minus the particle
-    // itself, stored to the masks and the row table.
-    auto close_row = [&](int r, uint32_t jb0, uint32_t je0, uint32_t dm, uint32_t ez, uint32_t sm) {
-        const uint32_t so = k - jb0;
+    // The words of chunk c of row r (bit b = candidate jb0 + 32c + b) minus
+    // the particle itself, stored to the masks and the row table.
+    auto close_chunk = [&](int r, uint32_t c, uint32_t jb0, uint32_t len, uint32_t dm, uint32_t ez, uint32_t sm) {
+        const uint32_t so = k - (jb0 + 32u * c);
         const uint32_t notself = (so < 32u) ? ~(1u << so) : ~0u;
         dm &= notself;
-        if (SKIN) mask[(size_t)r * mask_stride + k] = sm & notself;
-        mask[(size_t)(9 + r) * mask_stride + k] = dm & ~ez;
-        const uint32_t len = je0 - jb0;
-        const bool f = len > 32u;
-        const uint32_t v = f ? len : dm;
+        if (SKIN && len <= 32u) mask[(size_t)(SPH_MASK_SKIN + r) * mask_stride + k] = sm & notself;
+        mask[(size_t)(SPH_MASK_EXACT + 2 * r + c) * mask_stride + k] = dm & ~ez;
+        if (c == 0u) tab[r * ts] = jb0;
+        tab[(9 + 2 * r + c) * ts] = dm;
+        if (dm) live |= 1u << (2 * r + c);
+    };
+    // A row longer than 64 candidates: no words, phase 2 tests every candidate.
+    auto long_row = [&](int r, uint32_t jb0, uint32_t len) {
         tab[r * ts] = jb0;
-        tab[(9 + r) * ts] = v;
-        if (f) full |= 1u << r;
-        if (v) live |= 1u << r;
+        tab[(9 + 2 * r) * ts] = len;
+        full |= 1u << (2 * r);
+        live |= 1u << (2 * r);
     };
     if (WALK == 1) {
 #pragma unroll 1
         for (int r = 0; r < 9; ++r) {
             uint32_t jb0, je0;
             if (!row_range(pp, start, sc.cell_base, delta, g, r, jb0, je0)) continue;
-            uint32_t dm = 0u, ez = 0u, sm = 0u, bit = 1u;
-            uint32_t jj = jb0;
-            for (; jj + 2u <= je0; jj += 2u) {
-                const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
-                visit(q0, bit, dm, ez, sm);
-                visit(q1, bit << 1, dm, ez, sm);
-                bit <<= 2;
-            }
-            if (jj < je0) visit(__ldg(P1 + jj), bit, dm, ez, sm);
-            close_row(r, jb0, je0, dm, ez, sm);
+            const uint32_t len = je0 - jb0;
+            if (len > SPH_WIDE_ROW) { long_row(r, jb0, len); continue; }
+            uint32_t cb = jb0, c = 0u;
+            do {
+                const uint32_t ce = min(cb + 32u, je0);
+                uint32_t dm = 0u, ez = 0u, sm = 0u, bit = 1u;
+                uint32_t jj = cb;
+                for (; jj + 2u <= ce; jj += 2u) {
+                    const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
+                    visit(q0, bit, dm, ez, sm);
+                    visit(q1, bit << 1, dm, ez, sm);
+                    bit <<= 2;
+                }
+                if (jj < ce) visit(__ldg(P1 + jj), bit, dm, ez, sm);
+                close_chunk(r, c, jb0, len, dm, ez, sm);
+                cb += 32u;
+                ++c;
+            } while (cb < je0);
         }
     } else {
-        // one loop across all 9 rows, so lanes do not wait at row ends
+        // one loop across all 9 rows and their chunks, so lanes do not wait at
+        // row ends
         int r = -1;
-        uint32_t jb = 0, j = 0, je = 0, dm = 0u, ez = 0u, sm = 0u, bit = 0u;
+        uint32_t jb = 0, je = 0, j = 0, cend = 0, c = 0, len = 0, dm = 0u, ez = 0u, sm = 0u, bit = 0u;
         bool valid = false;
         for (;;) {
-            if (j >= je) {
-                if (valid) close_row(r, jb, je, dm, ez, sm);
+            if (j >= cend) {
+                if (valid) {
+                    close_chunk(r, c, jb, len, dm, ez, sm);
+                    if (j < je) {   // the row's second chunk
+                        ++c;
+                        cend = min(j + 32u, je);
+                        dm = ez = sm = 0u;
+                        bit = 1u;
+                        continue;
+                    }
+                }
                 if (++r >= 9) break;
-                dm = ez = sm = 0u;
-                bit = 1u;
                 valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
                 if (!valid) jb = je = 0;
+                len = je - jb;
+                if (valid && len > SPH_WIDE_ROW) {
+                    long_row(r, jb, len);
+                    valid = false;
+                    j = cend = 0;
+                    continue;
+                }
+                c = 0u;
                 j = jb;
+                cend = min(jb + 32u, je);
+                dm = ez = sm = 0u;
+                bit = 1u;
                 continue;
             }
             visit(__ldg(P1 + j), bit, dm, ez, sm);
@@ -460,16 +492,16 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
             }
         }
     };
-    // exact neighbours recorded by the density pass (mask words 9-17)
+    // exact neighbours recorded by the density pass (SPH_MASK_EXACT words)
     if constexpr (TABLE) {
         extern __shared__ uint32_t s_rows[];
         uint32_t live, full;
-        build_row_table(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k,
+        build_row_table(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k,
                         s_rows + threadIdx.x, blockDim.x, live, full);
         TableWalk walk(s_rows + threadIdx.x, blockDim.x, live, full);
         run(walk);
     } else {
-        MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
+        WideMaskWalk walk(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k);
         run(walk);
     }
     N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
@@ -581,16 +613,16 @@ k_force_integrate(const DevParams* __restrict__ params,
                 }
             }
         };
-        // exact neighbours recorded by the density pass (mask words 9-17)
+        // exact neighbours recorded by the density pass (SPH_MASK_EXACT words)
         if constexpr (TABLE) {
             extern __shared__ uint32_t s_rows[];
             uint32_t live, full;
-            build_row_table(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k,
+            build_row_table(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k,
                             s_rows + threadIdx.x, blockDim.x, live, full);
             TableWalk walk(s_rows + threadIdx.x, blockDim.x, live, full);
             run(walk);
         } else {
-            MaskWalk walk(pp, start, sc.cell_base, delta, g, mask + 9 * mask_stride, mask_stride, k);
+            WideMaskWalk walk(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k);
             run(walk);
         }
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
@@ -896,7 +928,7 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
     const bool rows = (a.variant & SPH_VARIANT_DENSITY_ROWS) != 0u;
     auto kern = a.skin_masks ? (rows ? k_density<1, true> : k_density<0, true>)
                              : (rows ? k_density<1, false> : k_density<0, false>);
-    const size_t smem = (size_t)18 * a.block * sizeof(uint32_t);   // the row table
+    const size_t smem = (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t);   // the row table
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
                                             a.V1, a.okey1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
@@ -911,7 +943,7 @@ cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t n
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
     const bool table = (a.variant & SPH_VARIANT_NORMALS_TABLE) != 0u;
     auto kern = table ? k_normals<true> : k_normals<false>;
-    const size_t smem = table ? (size_t)18 * a.block * sizeof(uint32_t) : 0;
+    const size_t smem = table ? (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t) : 0;
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
                                             a.N, a.ntiles, ctr(a, 1));
     return cudaGetLastError();
@@ -924,7 +956,7 @@ cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
                              : (occ ? k_force_integrate<true, 4, false> : k_force_integrate<true, 3, false>))
                     : (table ? (occ ? k_force_integrate<false, 4, true> : k_force_integrate<false, 3, true>)
                              : (occ ? k_force_integrate<false, 4, false> : k_force_integrate<false, 3, false>));
-    const size_t smem = table ? (size_t)18 * a.block * sizeof(uint32_t) : 0;
+    const size_t smem = table ? (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t) : 0;
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.Vc, a.A1, a.S, a.N, a.mask,
                                             a.mask_stride, a.P0, a.V2, a.A0, a.skin_masks ? a.maxdisp : nullptr,
                                             a.okey, a.pend, a.dbg_forces,

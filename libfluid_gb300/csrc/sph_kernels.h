@@ -24,8 +24,8 @@ struct StepArgs {
     uint32_t *count, *start, *scan_sums;
     uint32_t *key, *slot, *tmp, *perm;
     uint32_t *status;
-    uint32_t *mask;            // 18 neighbour-mask words per slot, word r at mask[r*mask_stride + slot]:
-                               // 0-8 skin radius (XSPH), 9-17 exact neighbours (normals, forces)
+    uint32_t *mask;            // SPH_MASK_ROWS neighbour-mask words per slot, word m at mask[m*mask_stride + slot]:
+                               // SPH_MASK_SKIN skin radius (XSPH), SPH_MASK_EXACT exact neighbours (normals, forces)
     size_t mask_stride;
     uint32_t *maxdisp;         // largest (displacement/h)^2 of the substep, float bits
     uint32_t block;            // threads per block = particles per tile
@@ -39,9 +39,10 @@ struct StepArgs {
 };
 
 // Shared-memory carveout (percent of the SM's maximum) requested for the
-// kernels that keep a row table in shared memory.
+// kernels that keep a row table in shared memory: the smallest that holds
+// the tables of 8 blocks of 128 threads, so that L1 keeps the rest.
 #ifndef SPH_TABLE_CARVEOUT_PCT
-#define SPH_TABLE_CARVEOUT_PCT 40
+#define SPH_TABLE_CARVEOUT_PCT 50
 #endif
 // One-time per-device kernel attributes (call before the first launch).
 cudaError_t init_kernel_attributes();

@@ -52,6 +52,17 @@ struct DevParams {
 // the device; otherwise XSPH walks all candidates).
 #define SPH_SKIN_DEFAULT 0.1f
 
+// Neighbour-mask rows per slot (row m of slot k at mask[m * stride + k]).
+// Exact-neighbour words of a cell row: rows of up to 64 candidates carry two
+// words (word h: candidates jb + 32h .. jb + 32h + 31; the second is written
+// and read only for rows longer than 32); longer rows carry none and are
+// walked in full.  Words of row r sit at mask rows SPH_MASK_EXACT + 2r + h.
+#define SPH_MASK_SKIN   0u    // 9 rows: candidates within the skin radius (rows of <= 32)
+#define SPH_MASK_EXACT  9u    // 18 rows: exact neighbours eps < r^2 <= h^2, j != i
+#define SPH_MASK_ROWS   27u
+#define SPH_WIDE_ROW    64u   // longest row with mask words
+#define SPH_ROW_TABLE_WORDS 27u   // per-thread row table: 9 row starts + 18 words
+
 // Kernel variants (bits of the execution config's `variant`). All variants
 // visit neighbours in the same order and give identical results; they differ
 // only in how the walk is scheduled.
