@@ -238,14 +238,15 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 //
 // Phase 1 scans the candidates of the 27 cells, 32 at a time, with the
 // distance test alone and records a bit per candidate within h (density
-// pairs), within eps (coincident) and, with SKIN, within the skin radius.  The
-// words go to the neighbour masks of the later passes (SPH_MASK_SKIN rows for
-// rows of up to 32 candidates; SPH_MASK_EXACT rows, two words per row of up to
-// 64: the exact neighbours eps < r^2 <= h^2, j != i) and to a row table in
-// shared memory (build_row_table's layout).  Phase 2 walks that table and
-// does the kernel arithmetic for the density pairs only (about one candidate
-// in six), so a warp no longer runs the neighbour path on every candidate
-// that any of its lanes accepts.  Rows longer than 64 candidates are not
+// pairs, j != i) and, with SKIN, within the skin radius.  The words go to the
+// neighbour masks of the later passes (SPH_MASK_SKIN rows for rows of up to
+// 32 candidates; SPH_MASK_EXACT rows, two words per row of up to 64) and to a
+// row table in shared memory (build_row_table's layout).  Coincident pairs
+// (r^2 <= eps) stay in the words: the density sum and XSPH take them, and the
+// normal and force passes drop them with their own r^2 > eps test.  Phase 2
+// walks that table and does the kernel arithmetic for the density pairs only
+// (about one candidate in six), so a warp no longer runs the neighbour path
+// on every candidate that any of its lanes accepts.  Rows longer than 64 candidates are not
 // scanned in phase 1; phase 2 walks them in full with the test.  Both phases
 // visit candidates in the reference's order, so the sum is the
 // candidate-order sum.  WALK selects phase 1's loop: flattened across the
@@ -302,21 +303,20 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     uint32_t live = 0u, full = 0u;
 
     // ---- phase 1: distance test of every candidate ----
-    auto visit = [&](const float4& q, uint32_t bit, uint32_t& dm, uint32_t& ez, uint32_t& sm) {
+    auto visit = [&](const float4& q, uint32_t bit, uint32_t& dm, uint32_t& sm) {
         const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
         if (rr <= h2) dm |= bit;
-        if (rr <= eps) ez |= bit;
         if (SKIN && rr <= skin2) sm |= bit;
     };
     // The words of chunk c of row r (bit b = candidate jb0 + 32c + b) minus
     // the particle itself, stored to the masks and the row table.
-    auto close_chunk = [&](int r, uint32_t c, uint32_t jb0, uint32_t len, uint32_t dm, uint32_t ez, uint32_t sm) {
+    auto close_chunk = [&](int r, uint32_t c, uint32_t jb0, uint32_t len, uint32_t dm, uint32_t sm) {
         const uint32_t so = k - (jb0 + 32u * c);
         const uint32_t notself = (so < 32u) ? ~(1u << so) : ~0u;
         dm &= notself;
         if (SKIN && len <= 32u) mask[(size_t)(SPH_MASK_SKIN + r) * mask_stride + k] = sm & notself;
-        mask[(size_t)(SPH_MASK_EXACT + 2 * r + c) * mask_stride + k] = dm & ~ez;
+        mask[(size_t)(SPH_MASK_EXACT + 2 * r + c) * mask_stride + k] = dm;
         if (c == 0u) tab[r * ts] = jb0;
         tab[(9 + 2 * r + c) * ts] = dm;
         if (dm) live |= 1u << (2 * r + c);
@@ -338,16 +338,16 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
             uint32_t cb = jb0, c = 0u;
             do {
                 const uint32_t ce = min(cb + 32u, je0);
-                uint32_t dm = 0u, ez = 0u, sm = 0u, bit = 1u;
+                uint32_t dm = 0u, sm = 0u, bit = 1u;
                 uint32_t jj = cb;
                 for (; jj + 2u <= ce; jj += 2u) {
                     const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
-                    visit(q0, bit, dm, ez, sm);
-                    visit(q1, bit << 1, dm, ez, sm);
+                    visit(q0, bit, dm, sm);
+                    visit(q1, bit << 1, dm, sm);
                     bit <<= 2;
                 }
-                if (jj < ce) visit(__ldg(P1 + jj), bit, dm, ez, sm);
-                close_chunk(r, c, jb0, len, dm, ez, sm);
+                if (jj < ce) visit(__ldg(P1 + jj), bit, dm, sm);
+                close_chunk(r, c, jb0, len, dm, sm);
                 cb += 32u;
                 ++c;
             } while (cb < je0);
@@ -356,16 +356,16 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         // one loop across all 9 rows and their chunks, so lanes do not wait at
         // row ends
         int r = -1;
-        uint32_t jb = 0, je = 0, j = 0, cend = 0, c = 0, len = 0, dm = 0u, ez = 0u, sm = 0u, bit = 0u;
+        uint32_t jb = 0, je = 0, j = 0, cend = 0, c = 0, len = 0, dm = 0u, sm = 0u, bit = 0u;
         bool valid = false;
         for (;;) {
             if (j >= cend) {
                 if (valid) {
-                    close_chunk(r, c, jb, len, dm, ez, sm);
+                    close_chunk(r, c, jb, len, dm, sm);
                     if (j < je) {   // the row's second chunk
                         ++c;
                         cend = min(j + 32u, je);
-                        dm = ez = sm = 0u;
+                        dm = sm = 0u;
                         bit = 1u;
                         continue;
                     }
@@ -383,11 +383,11 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                 c = 0u;
                 j = jb;
                 cend = min(jb + 32u, je);
-                dm = ez = sm = 0u;
+                dm = sm = 0u;
                 bit = 1u;
                 continue;
             }
-            visit(__ldg(P1 + j), bit, dm, ez, sm);
+            visit(__ldg(P1 + j), bit, dm, sm);
             bit <<= 1;
             ++j;
         }

@@ -58,7 +58,7 @@ struct DevParams {
 // and read only for rows longer than 32); longer rows carry none and are
 // walked in full.  Words of row r sit at mask rows SPH_MASK_EXACT + 2r + h.
 #define SPH_MASK_SKIN   0u    // 9 rows: candidates within the skin radius (rows of <= 32)
-#define SPH_MASK_EXACT  9u    // 18 rows: exact neighbours eps < r^2 <= h^2, j != i
+#define SPH_MASK_EXACT  9u    // 18 rows: neighbours r^2 <= h^2, j != i (readers test r^2 > eps)
 #define SPH_MASK_ROWS   27u
 #define SPH_WIDE_ROW    64u   // longest row with mask words
 #define SPH_ROW_TABLE_WORDS 27u   // per-thread row table: 9 row starts + 18 words
