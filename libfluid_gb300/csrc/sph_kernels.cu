@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // scanned in phase 1; phase 2 walks them in full with the test.  Both phases
 // visit candidates in the reference's order, so the sum is the
 // candidate-order sum.  WALK selects phase 1's loop: flattened across the
-// rows (0) or one loop per row with two loads in flight (1); the words are
+// rows (0) or one loop per row with four loads in flight (1); the words are
 // the same.
 //
 // Deferred XSPH.  For a scene whose previous substep ended without its XSPH
@@ -328,11 +328,24 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         full |= 1u << (2 * r);
         live |= 1u << (2 * r);
     };
+    // The 9 row ranges, loaded together (18 independent loads) into the row
+    // table; a row's end sits in its first word's entry until the scan of
+    // the row replaces it.
+    uint32_t rows = 0u;
+#pragma unroll
+    for (int r = 0; r < 9; ++r) {
+        uint32_t jb0, je0;
+        if (row_range(pp, start, sc.cell_base, delta, g, r, jb0, je0)) {
+            rows |= 1u << r;
+            tab[r * ts] = jb0;
+            tab[(9 + 2 * r) * ts] = je0;
+        }
+    }
     if (WALK == 1) {
 #pragma unroll 1
         for (int r = 0; r < 9; ++r) {
-            uint32_t jb0, je0;
-            if (!row_range(pp, start, sc.cell_base, delta, g, r, jb0, je0)) continue;
+            if (!((rows >> r) & 1u)) continue;
+            const uint32_t jb0 = tab[r * ts], je0 = tab[(9 + 2 * r) * ts];
             const uint32_t len = je0 - jb0;
             if (len > SPH_WIDE_ROW) { long_row(r, jb0, len); continue; }
             uint32_t cb = jb0, c = 0u;
@@ -340,11 +353,21 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                 const uint32_t ce = min(cb + 32u, je0);
                 uint32_t dm = 0u, sm = 0u, bit = 1u;
                 uint32_t jj = cb;
-                for (; jj + 2u <= ce; jj += 2u) {
+                for (; jj + 4u <= ce; jj += 4u) {
+                    const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
+                    const float4 q2 = __ldg(P1 + jj + 2u), q3 = __ldg(P1 + jj + 3u);
+                    visit(q0, bit, dm, sm);
+                    visit(q1, bit << 1, dm, sm);
+                    visit(q2, bit << 2, dm, sm);
+                    visit(q3, bit << 3, dm, sm);
+                    bit <<= 4;
+                }
+                if (jj + 2u <= ce) {
                     const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
                     visit(q0, bit, dm, sm);
                     visit(q1, bit << 1, dm, sm);
                     bit <<= 2;
+                    jj += 2u;
                 }
                 if (jj < ce) visit(__ldg(P1 + jj), bit, dm, sm);
                 close_chunk(r, c, jb0, len, dm, sm);
@@ -371,8 +394,9 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                     }
                 }
                 if (++r >= 9) break;
-                valid = row_range(pp, start, sc.cell_base, delta, g, r, jb, je);
-                if (!valid) jb = je = 0;
+                valid = ((rows >> r) & 1u) != 0u;
+                jb = valid ? tab[r * ts] : 0u;
+                je = valid ? tab[(9 + 2 * r) * ts] : 0u;
                 len = je - jb;
                 if (valid && len > SPH_WIDE_ROW) {
                     long_row(r, jb, len);
