@@ -428,7 +428,15 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     TableWalk walk(tab, ts, live, full);
     uint32_t j;
     while (walk.next(j)) {
+        // the pair's XSPH operands are loaded with its position, before any
+        // test, so that the three latencies overlap
         const float4 q = __ldg(P1 + j);
+        float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
+        uint32_t oj = SPH_OKEY_NULL;
+        if (xs) {
+            vj = __ldg(V1 + j);
+            oj = __ldg(okey1 + j);
+        }
         const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
         // true for every recorded bit; the test matters in rows walked in full
@@ -439,8 +447,6 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
             sum = fmaf(mass, w, sum);
             cnt++;
             if (xs) {
-                const float4 vj = __ldg(V1 + j);
-                const uint32_t oj = __ldg(okey1 + j);
                 const float rs = p.w + q.w;   // the previous substep's densities
                 if (rs > eps && cells_adjacent_fast(oi, oj)) {
                     const float coeff = w * __fdividef(pp.two_mass, rs);
