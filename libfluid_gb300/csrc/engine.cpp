@@ -107,6 +107,8 @@ Engine::Engine(int device) {
     else device_ = device;
     cudaSetDevice(device_);
     cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
+    cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&copy_ev_, cudaEventDisableTiming);
     cudaMallocHost((void**)&h_status_, sizeof(uint32_t));
     cudaMalloc((void**)&status_, sizeof(uint32_t));
     cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_);
@@ -119,6 +121,7 @@ Engine::Engine(int device) {
 Engine::~Engine() {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
+    if (copy_stream_) cudaStreamSynchronize(copy_stream_);
     free_all();
     if (exec_pre_) cudaGraphExecDestroy(exec_pre_);
     if (exec_suf_) cudaGraphExecDestroy(exec_suf_);
@@ -130,6 +133,8 @@ Engine::~Engine() {
     if (scal_) cudaFree(scal_);
     if (h_status_) cudaFreeHost(h_status_);
     if (h_params_) cudaFreeHost(h_params_);
+    if (copy_ev_) cudaEventDestroy(copy_ev_);
+    if (copy_stream_) cudaStreamDestroy(copy_stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -290,7 +295,7 @@ void Engine::free_slots(uint32_t base, uint32_t n) {
 
 int Engine::staging(size_t bytes, float** out) {
     if (bytes > stage_bytes_) {
-        if (stage_) { cudaStreamSynchronize(stream_); cudaFree(stage_); }
+        if (stage_) { cudaStreamSynchronize(stream_); cudaStreamSynchronize(copy_stream_); cudaFree(stage_); }
         stage_ = nullptr;
         stage_bytes_ = 0;
         ENG_CK(cudaMalloc((void**)&stage_, bytes), "staging alloc");
@@ -628,16 +633,20 @@ int Engine::step(uint32_t substeps, bool sync) {
 
 // Run the next substep's prefix once, for reads of scenes whose XSPH update
 // is pending: its density pass computes the updated velocities (Vc); the next
-// step() starts from the suffix, so the work is not repeated.
-int Engine::ensure_prefix() {
+// step() starts from the suffix, so the work is not repeated.  With
+// wait = false the caller reads the status word (read_status) afterwards and
+// clears prefix_valid_ if it reports an error.
+int Engine::ensure_prefix(bool wait) {
     if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
     if (prefix_valid_) return ENG_OK;
     int rc = prepare();
     if (rc) return rc;
     if (use_graph_ && !profiling_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
     else { rc = launch_prefix(false); if (rc) return rc; }
-    rc = read_status();
-    if (rc) return rc;
+    if (wait) {
+        rc = read_status();
+        if (rc) return rc;
+    }
     prefix_valid_ = true;
     return ENG_OK;
 }
@@ -646,7 +655,7 @@ int Engine::ensure_prefix() {
 // the others hold no particles then): a read of one scene of many costs that
 // scene's share.  Scene-local, so its values equal a full prefix's; the full
 // prefix is not valid afterwards.
-int Engine::prefix_scene(const Scene& sc) {
+int Engine::prefix_scene(const Scene& sc, bool wait) {
     int rc = prepare();
     if (rc) return rc;
     StepArgs a = args();
@@ -657,7 +666,7 @@ int Engine::prefix_scene(const Scene& sc) {
     rc = launch_prefix_args(a, false);
     if (rc) return rc;
     prefix_valid_ = false;
-    return read_status();
+    return wait ? read_status() : ENG_OK;
 }
 
 // Write a pending XSPH update into the state (V0) and clear it.  A fresh
@@ -802,14 +811,17 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     // velocities (cell order), read back into state order; the state itself
     // is not changed, so reading never alters the trajectory.
     const bool pend = s->pending && vel;
-    if (pend) {
-        // one scene of several, and no full prefix at hand: that scene's prefix only
+    // one scene of several, and no full prefix at hand: that scene's prefix only
+    auto run_prefix = [&](bool wait) {
         if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
-        int rc = (prefix_valid_ || scenes_.size() == 1) ? ensure_prefix() : prefix_scene(*s);
+        return (prefix_valid_ || scenes_.size() == 1) ? ensure_prefix(wait) : prefix_scene(*s, wait);
+    };
+    if (pend && to_device) {
+        int rc = run_prefix(true);
         if (rc) return rc;
     }
-    const StepArgs a = args();
     if (to_device) {
+        const StepArgs a = args();
         ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, pos, colour, pend ? nullptr : vel,
                            stream_), "pack");
         if (pend) ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, vel, nullptr, false,
@@ -829,12 +841,32 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     float* dv = vel ? st + (size_t)n * 6 : nullptr;
     ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, pend ? nullptr : dv, stream_),
            "pack");
-    if (pend) ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, dv, nullptr, false, stream_),
-                     "unsort");
-    if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, stream_), "download");
-    if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, stream_), "download");
-    if (vel) ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
-    ENG_CK(cudaStreamSynchronize(stream_), "download sync");
+    if (!pend) {
+        if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+        if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+        if (vel) ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+        ENG_CK(cudaStreamSynchronize(stream_), "download sync");
+        return ENG_OK;
+    }
+    // Positions and colours do not depend on the pending XSPH update (the
+    // prefix reads P0 and does not write it): they cross the host link on the
+    // copy stream while the prefix computes the velocities.
+    ENG_CK(cudaEventRecord(copy_ev_, stream_), "export event");
+    ENG_CK(cudaStreamWaitEvent(copy_stream_, copy_ev_, 0), "export wait");
+    if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
+    if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
+    rc = run_prefix(false);
+    if (rc == ENG_OK) {
+        const StepArgs a = args();
+        ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, dv, nullptr, false, stream_),
+               "unsort");
+        ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+    }
+    const cudaError_t ce = cudaStreamSynchronize(copy_stream_);
+    if (rc) return rc;
+    if (ce != cudaSuccess) return cuda_fail(ce, "download sync");
+    rc = read_status();   // the prefix's status; waits for the velocity copy too
+    if (rc) { prefix_valid_ = false; return rc; }
     return ENG_OK;
 }
 

@@ -133,9 +133,9 @@ private:
     int upload_params();
     int launch_prefix(bool profile);   // memsets, hash, scan, sort, density
     int launch_prefix_args(const StepArgs& a, bool profile);
-    int prefix_scene(const Scene& s);  // the prefix over one scene's tiles
+    int prefix_scene(const Scene& s, bool wait = true);  // the prefix over one scene's tiles
     int launch_suffix(bool profile);   // normals, force + integrator, [XSPH]
-    int ensure_prefix();               // the next substep's prefix, computed once
+    int ensure_prefix(bool wait = true);   // the next substep's prefix, computed once
     int materialize(Scene& s);         // apply a pending XSPH update to the state
     int materialize_all();
     void clear_pending(Scene& s);      // state replaced: nothing pending
@@ -154,6 +154,8 @@ private:
 
     int device_ = 0;
     cudaStream_t stream_ = nullptr;
+    cudaStream_t copy_stream_ = nullptr;   // exports: copies that overlap the prefix
+    cudaEvent_t copy_ev_ = nullptr;
     std::string err_;
     std::vector<Scene> scenes_;
     int next_id_ = 1;
