@@ -244,7 +244,8 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
         count_ = start_ = scan_sums_ = nullptr;
         cudaError_t e1 = cudaMalloc((void**)&count_, nc * sizeof(uint32_t));
         cudaError_t e2 = cudaMalloc((void**)&start_, (nc + 1) * sizeof(uint32_t));
-        cudaError_t e3 = cudaMalloc((void**)&scan_sums_, (nc / 4096 + 2) * sizeof(uint32_t));
+        // the scan's tile counter and look-back descriptors (64-bit words)
+        cudaError_t e3 = cudaMalloc((void**)&scan_sums_, (nc / 4096 + 3) * sizeof(unsigned long long));
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
             return fail(ENG_ENOMEM, "device allocation of cell arrays failed");
         ccap_ = nc;
@@ -548,6 +549,7 @@ int Engine::read_status() {
         if (st & SPH_STATUS_CELL_OVERFLOW)
             return fail(ENG_ECELL, "a grid cell held more than 8192 particles");
         if (st & SPH_STATUS_NONFINITE) return fail(ENG_ENAN, "non-finite particle position");
+        if (st & SPH_STATUS_SCAN_TIMEOUT) return fail(ENG_ETIMEOUT, "cell scan: a look-back wait ran out");
     }
     return ENG_OK;
 }

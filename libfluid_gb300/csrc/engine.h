@@ -52,7 +52,7 @@ struct Scene {
     uint32_t table_index = 0, tile_first = 0, tile_count = 0;
 };
 
-enum { ENG_OK = 0, ENG_EINVAL = 1, ENG_ENOMEM = 2, ENG_ECUDA = 3, ENG_ENAN = 4, ENG_ECELL = 7 };
+enum { ENG_OK = 0, ENG_EINVAL = 1, ENG_ENOMEM = 2, ENG_ECUDA = 3, ENG_ENAN = 4, ENG_ETIMEOUT = 5, ENG_ECELL = 7 };
 
 class Engine {
 public:

@@ -166,6 +166,128 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
     }
 }
 
+// Single-pass form of the same scan, used by the substep: decoupled
+// look-back (Merrill and Garland, "Single-pass Parallel Prefix Scan with
+// Decoupled Look-back", NVIDIA technical report NVR-2016-002).  Each tile
+// publishes its aggregate, then adds the aggregates of the tiles before it
+// until it meets one that has published its inclusive prefix, and publishes
+// its own.  A descriptor is one 64-bit word (flag << 32 | value), so flag and
+// value are read together.  desc[0] hands out tile numbers in the order the
+// blocks start, so every tile waited on belongs to a block that is already
+// running and waits only on tiles before it; the waits are bounded all the
+// same (SPH_STATUS_SCAN_TIMEOUT, the outputs are then invalid).
+constexpr unsigned long long SCAN_AGG = 1ull << 32;
+constexpr unsigned long long SCAN_PRE = 2ull << 32;
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(const uint32_t* __restrict__ in, uint32_t n,
+                                                              unsigned long long* __restrict__ desc,
+                                                              uint32_t* __restrict__ out,
+                                                              uint32_t* __restrict__ status) {
+    __shared__ uint32_t s_tile, s_prefix, s_total;
+    __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
+    if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(desc), 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    const bool whole = base + SCAN_ITEMS <= n;   // 16 counts, 64-byte aligned
+    uint32_t v[SCAN_ITEMS];
+    if (whole) {
+        const uint4* p4 = reinterpret_cast<const uint4*>(in + base);
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
+            const uint4 w = __ldg(p4 + q);
+            v[4 * q] = w.x; v[4 * q + 1] = w.y; v[4 * q + 2] = w.z; v[4 * q + 3] = w.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (base + k < n) ? __ldg(in + base + k) : 0u;
+    }
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) s += v[k];
+    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t inc = warp_incl_scan(s);
+    if (lane == 31) warp_tot[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t w = (lane < SCAN_THREADS / 32) ? warp_tot[lane] : 0u;
+        const uint32_t wi = warp_incl_scan(w);
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = wi - w;
+        if (lane == 31) s_total = wi;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const uint32_t agg = s_total;
+        uint32_t excl = 0;
+        if (tile == 0) {
+            if (lane == 0) st_relaxed_u64(desc + 1, SCAN_PRE | agg);
+        } else {
+            if (lane == 0) st_relaxed_u64(desc + 1 + tile, SCAN_AGG | agg);
+            int j = (int)tile - 1;   // lane l reads tile j - l
+            for (;;) {
+                const int idx = j - (int)lane;
+                unsigned long long d = SCAN_PRE;   // before tile 0: an empty prefix
+                if (idx >= 0) {
+                    uint32_t spins = 0;
+                    d = ld_relaxed_u64(desc + 1 + idx);
+                    while ((d >> 32) == 0ull) {
+                        if (++spins > SCAN_SPIN_LIMIT) {
+                            atomicOr(status, SPH_STATUS_SCAN_TIMEOUT);
+                            d = SCAN_PRE;
+                            break;
+                        }
+                        __nanosleep(32);
+                        d = ld_relaxed_u64(desc + 1 + idx);
+                    }
+                }
+                const unsigned pre = __ballot_sync(0xffffffffu, (d >> 32) == 2ull);
+                const int stop = pre ? __ffs(pre) - 1 : 31;   // lanes 0..stop contribute
+                uint32_t val = ((int)lane <= stop) ? (uint32_t)d : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                excl += val;
+                if (pre) break;
+                j -= 32;
+            }
+            if (lane == 0) st_relaxed_u64(desc + 1 + tile, SCAN_PRE | (excl + agg));
+        }
+        if (lane == 0) s_prefix = excl;
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + warp_tot[warp] + inc - s;
+    if (whole) {
+        uint4* o4 = reinterpret_cast<uint4*>(out + base);
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
+            uint4 w;
+            w.x = run; run += v[4 * q];
+            w.y = run; run += v[4 * q + 1];
+            w.z = run; run += v[4 * q + 2];
+            w.w = run; run += v[4 * q + 3];
+            o4[q] = w;
+        }
+        if (base + SCAN_ITEMS == n) out[n] = run;   // total after the last cell
+    } else {
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; ++k) {
+            const uint32_t idx = base + k;
+            if (idx < n) out[idx] = run;
+            run += v[k];
+            if (idx + 1 == n) out[n] = run;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Scatter: provisional slot of each particle in cell order.
 // ---------------------------------------------------------------------------
@@ -930,13 +1052,16 @@ cudaError_t init_kernel_attributes() {
     return cudaSuccess;
 }
 
+// a.scan_sums holds nt + 1 64-bit words: the tile counter, then one
+// look-back descriptor per tile; both start at zero.
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
     const uint32_t n = a.total_cells;
+    if (n == 0) return cudaErrorInvalidValue;
     const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
-    if (nt > 1024u * 32u) return cudaErrorInvalidValue;
-    k_scan_reduce<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, a.scan_sums);
-    k_scan_top<<<1, 1024, 0, st>>>(a.scan_sums, nt);
-    k_scan_down<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, a.scan_sums, a.start);
+    unsigned long long* desc = reinterpret_cast<unsigned long long*>(a.scan_sums);
+    cudaError_t e = cudaMemsetAsync(desc, 0, (size_t)(nt + 1) * sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, desc, a.start, a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,

@@ -90,6 +90,7 @@ struct DevScene {
 // Status bits raised by kernels (read back after a step).
 #define SPH_STATUS_CELL_OVERFLOW 0x1u   // a cell held more particles than the rank pass supports
 #define SPH_STATUS_NONFINITE     0x2u   // a non-finite position appeared
+#define SPH_STATUS_SCAN_TIMEOUT  0x4u   // a wait of the cell scan's look-back ran out
 
 // Maximum particles one cell (or a scene's NULL bucket) may hold.  The
 // reference cannot launch more than 1024 threads per cell block
