@@ -289,6 +289,10 @@ int sph_batch_set_exec(sph_batch* b, const sph_exec_config* e);
 int sph_batch_set_deferred_xsph(sph_batch* b, int on);
 int sph_batch_timer_mark(sph_batch* b, int slot);
 int sph_batch_timer_elapsed(sph_batch* b, int a, int b2, float* ms);
+/* Per-pass CUDA-event timing of the batch's substeps, as sph_set_profiling /
+ * sph_get_pass_times: one launch per pass covers every scene. */
+int sph_batch_set_profiling(sph_batch* b, int on);
+int sph_batch_get_pass_times(sph_batch* b, double* ms, int cap, uint64_t* substeps);
 const char* sph_batch_last_error(const sph_batch* b);
 
 /* ---- served step (continuous batching) ----------------------------------

@@ -35,6 +35,8 @@ SIGNATURES = [
     ("sph_batch_set_exec", _I, [_P, _P]),
     ("sph_batch_set_deferred_xsph", _I, [_P, _I]),
     ("sph_batch_timer_mark", _I, [_P, _I]),
+    ("sph_batch_set_profiling", _I, [_P, _I]),
+    ("sph_batch_get_pass_times", _I, [_P, C.POINTER(C.c_double), _I, C.POINTER(C.c_uint64)]),
     ("sph_batch_timer_elapsed", _I, [_P, _I, _I, C.POINTER(_F)]),
     ("sph_batch_last_error", C.c_char_p, [_P]),
     ("sph_server_create", _I, [C.POINTER(_P), _P]),

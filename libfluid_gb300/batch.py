@@ -162,6 +162,17 @@ class Batch:
     def set_deferred_xsph(self, on: bool) -> None:
         self._ck(self._L.sph_batch_set_deferred_xsph(self._h, 1 if on else 0))
 
+    def set_profiling(self, on: bool) -> None:
+        """Per-pass CUDA events around each pass (replaces graph replay)."""
+        self._ck(self._L.sph_batch_set_profiling(self._h, 1 if on else 0))
+
+    def pass_times(self) -> tuple[dict, int]:
+        """Accumulated per-pass milliseconds and the substeps they cover."""
+        buf = (C.c_double * 8)()
+        n = C.c_uint64(0)
+        self._ck(self._L.sph_batch_get_pass_times(self._h, buf, 8, C.byref(n)))
+        return {self._L.sph_pass_name(i).decode(): buf[i] for i in range(8)}, n.value
+
     def timer_mark(self, slot: int) -> None:
         self._ck(self._L.sph_batch_timer_mark(self._h, slot))
 

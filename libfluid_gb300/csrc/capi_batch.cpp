@@ -200,6 +200,14 @@ int sph_batch_set_exec(sph_batch* b, const sph_exec_config* e) {
     x.variant = e->variant;
     return berr(b, b->eng->set_exec(x));
 }
+int sph_batch_set_profiling(sph_batch* b, int on) {
+    if (!b) return SPH_EINVAL;
+    return berr(b, b->eng->set_profiling(on != 0));
+}
+int sph_batch_get_pass_times(sph_batch* b, double* ms, int cap, uint64_t* substeps) {
+    if (!b || !ms) return SPH_EINVAL;
+    return berr(b, b->eng->get_pass_times(ms, cap, substeps));
+}
 int sph_batch_timer_mark(sph_batch* b, int slot) {
     if (!b) return SPH_EINVAL;
     return berr(b, b->eng->timer_mark(slot));
