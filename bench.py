@@ -298,8 +298,8 @@ def run_ours(args, dist):
     fs = FluidSystem(dist.local)
     configure(fs, spec, pos, vel)
     L = _capi.lib()
-    if args.variant is not None:
-        fs.setExec(variant=args.variant)
+    if args.variant is not None or args.tile is not None:
+        fs.setExec(tile=args.tile or 128, variant=31 if args.variant is None else args.variant)
 
     # ---- warm-up ----
     for _ in range(args.warmup):
@@ -580,6 +580,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-refcuda", action="store_true")
+    ap.add_argument("--tile", type=int, default=None, choices=[64, 128, 256],
+                    help="plain workload: particles per tile (threads per block; default: the compiled default)")
     ap.add_argument("--variant", type=int, default=None,
                     help="plain workload: kernel variant bits (SPH_VARIANT_*; default: the compiled default)")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
