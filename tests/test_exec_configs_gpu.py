@@ -10,10 +10,11 @@ from libfluid_gb300.batch import Batch
 pytestmark = pytest.mark.gpu
 
 
-def _run(specs, steps, graph=True, **exe):
+def _run(specs, steps, graph=True, deferred=True, **exe):
     b = Batch(0)
     b.set_exec(**exe)
     b.set_use_graph(graph)
+    b.set_deferred_xsph(deferred)
     ids = [b.add_scene(s) for s in specs]
     b.step(steps)
     out = [b.get_state(i) for i in ids]
@@ -55,3 +56,23 @@ def test_eager_equals_graph():
     a = _run(specs, 5, graph=True)
     b = _run(specs, 5, graph=False)
     assert np.array_equal(a[0][0], b[0][0]) and np.array_equal(a[0][2], b[0][2])
+
+
+@pytest.mark.parametrize("deferred", [True, False])
+@pytest.mark.parametrize("variant", [1, 2, 8, 16, 31])
+def test_variants_bit_identical_crowded(variant, deferred):
+    """The same on compressed lattices whose cell rows hold 33 to 160
+    candidates, so the two-word masks and the rows walked in full meet every
+    walk (the table walks and the mask walks of the normal and force passes,
+    both density loops, and, without deferral, the per-substep XSPH pass's
+    skin walks), with surface tension so the normal pass runs."""
+    specs = []
+    for k, spacing in enumerate((0.0075, 0.006)):
+        lat = W.Lattice(lo=(0.05, 0.05, 0.05), spacing=spacing, nx=20, ny=20, nz=20, jitter=0.05 * spacing,
+                        seed=41 + k)
+        specs.append(W.SceneSpec(box=(0.4, 0.4, 0.4), h=0.02, blocks=[lat], mass=1e-3, particle_size=0.005,
+                                 dt=1e-4, steps=4, surface_tension=0.05))
+    base = _run(specs, 4, deferred=deferred, tile=128, persistent=0, skin=0.1, variant=0)
+    other = _run(specs, 4, deferred=deferred, tile=128, persistent=0, skin=0.1, variant=variant)
+    for (pa, ca, va), (pb, cb, vb) in zip(base, other):
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
