@@ -540,7 +540,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     }
 
     // ---- phase 2: the density pairs, in candidate order ----
-    const float h = pp.h, mass = pp.mass, c6 = pp.poly6;
+    const float h = pp.h, mass = pp.mass, c6 = pp.poly6, two_m = pp.two_mass;
     float sum = 0.0f;
     uint32_t cnt = 0;
     // deferred XSPH of the previous substep (only for particles that had a cell then)
@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
             if (xs) {
                 const float rs = p.w + q.w;   // the previous substep's densities
                 if (rs > eps && cells_adjacent_fast(oi, oj)) {
-                    const float coeff = w * __fdividef(pp.two_mass, rs);
+                    const float coeff = w * __fdividef(two_m, rs);
                     ax = fmaf(coeff, vj.x - vi.x, ax);
                     ay = fmaf(coeff, vj.y - vi.y, ay);
                     az = fmaf(coeff, vj.z - vi.z, az);
@@ -627,6 +627,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
     // factor r of gradPoly6 cancels the 1/r; h^2 - r^2 is formed from the
     // rounded root r as gradPoly6 forms it (it cancels near r = h)
     const float mc = pp.mass * pp.grad_poly6;
+    const float h2 = pp.h2, eps = pp.eps, h = pp.h;
     auto run = [&](auto& walk) {
         uint32_t j;
         while (walk.next(j)) {
@@ -634,10 +635,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
             const float rhoj = __ldg(&S[j].x);
             const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-            if (r2 <= pp.h2 && r2 > pp.eps && j != k && rhoj > pp.eps) {
+            if (r2 <= h2 && r2 > eps && j != k && rhoj > eps) {
                 const float r = sqrtf(r2);
-                const float x = fmaf(-r, r, pp.h2);
-                const float s = (r >= pp.h) ? 0.0f : __fdividef(mc * (x * x), rhoj);
+                const float x = fmaf(-r, r, h2);
+                const float s = (r >= h) ? 0.0f : __fdividef(mc * (x * x), rhoj);
                 sx = fmaf(s, rx, sx);
                 sy = fmaf(s, ry, sy);
                 sz = fmaf(s, rz, sz);
@@ -721,6 +722,8 @@ k_force_integrate(const DevParams* __restrict__ params,
         const float tden = (2.0f * pp.rest_density) / (ri + ri);
         const float sm = -pp.surface_tension * pp.mass;
         const float coh_m = -pp.mass * pp.mass;
+        // per-scene constants of the pair loop, held in registers
+        const float visc = pp.viscosity, hh = pp.h, visc_eps = pp.visc_eps, mass = pp.mass, gsp = pp.grad_spiky;
         auto run = [&](auto& walk) {
             uint32_t j;
             while (walk.next(j)) {
@@ -741,12 +744,13 @@ k_force_integrate(const DevParams* __restrict__ params,
                     // artificial viscosity -visc (cs_i + cs_j) mu / (rho_i + rho_j),
                     // mu = h ux / (r^2 + 0.01 h^2), only for approaching pairs;
                     // evaluated without a branch (finite for every pair) and selected
-                    const float Pv = __fdividef(-pp.viscosity * (csi + sj.z) * (pp.h * ux),
-                                                (r2 + pp.visc_eps) * (ri + sj.x));
+                    const float Pv = __fdividef(-visc * (csi + sj.z) * (hh * ux),
+                                                (r2 + visc_eps) * (ri + sj.x));
                     const float Pi = (ux < 0.0f) ? Pv : 0.0f;
                     // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
                     const float mid = sj.y * inv_ri2 + pri * sj.w;
-                    const float sr = (pp.mass * grad_spiky(pp, r)) * inv_r;
+                    const float gspk = (r >= hh) ? 0.0f : gsp * (hh - r) * (hh - r);   // grad_spiky
+                    const float sr = (mass * gspk) * inv_r;
                     const float cx = sr * rx, cy = sr * ry, cz = sr * rz;
                     fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
                     const float mp = mid + Pi;
