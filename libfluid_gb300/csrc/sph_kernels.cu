@@ -368,10 +368,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // normal and force passes drop them with their own r^2 > eps test.  Phase 2
 // walks that table and does the kernel arithmetic for the density pairs only
 // (about one candidate in six), so a warp no longer runs the neighbour path
-// on every candidate that any of its lanes accepts.  Rows longer than 64 candidates are not
-// scanned in phase 1; phase 2 walks them in full with the test.  Both phases
-// visit candidates in the reference's order, so the sum is the
-// candidate-order sum.  WALK selects phase 1's loop: flattened across the
+// on every candidate that any of its lanes accepts.  Rows longer than 64
+// candidates are not scanned in phase 1; phase 2 walks them in full with the
+// test.  Both phases visit candidates in the reference's order, so the sum is
+// the candidate-order sum.  WALK selects phase 1's loop: flattened across the
 // rows (0) or one loop per row with four loads in flight (1); the words are
 // the same.
 //
