@@ -70,7 +70,10 @@ int sph_set_state(sph_system* s, const float* pos, const float* vel, uint32_t n)
  * reference's float loop `for (dt = part; dt <= full; dt += part)` would run
  * (e.g. advance(0.01, 10) runs 9), each with dt = full_dt/substeps.  Blocks
  * until the work is done.  *executed (may be NULL) receives the count.
- * A loop that would never terminate in the reference returns SPH_EINVAL. */
+ * A loop that would never terminate in the reference returns SPH_EINVAL.
+ * Without debug taps it then starts the next substep's sort and density
+ * pass before returning, which the next advance or an export needs; errors
+ * that pass raises are returned by the next call. */
 int sph_advance(sph_system* s, float full_dt, uint32_t substeps, uint32_t* executed);
 /* As sph_advance but returns after enqueueing; pair with sph_sync. */
 int sph_advance_async(sph_system* s, float full_dt, uint32_t substeps, uint32_t* executed);
@@ -190,7 +193,12 @@ enum sph_field {
     SPH_FIELD_ACC = 14,       /* f32[3n] m_Acceleration */
     SPH_FIELD_VEL_INT = 15    /* f32[3n] velocity after integration, before XSPH */
 };
-/* Enable the optional taps (neighbour counts, force components). */
+/* Enable the optional taps (neighbour counts, force components).  With taps
+ * on, every field describes the last substep run.  Without them, the sort
+ * fields (hash, perm, cell start and occupancy) and density, pressure and
+ * sound speed describe the most recent sort, which after a blocking advance
+ * or an export is already the next substep's (its prefix runs early, see
+ * sph_advance). */
 int sph_debug_enable(sph_system* s, int on);
 int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
 

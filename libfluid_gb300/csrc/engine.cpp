@@ -109,6 +109,7 @@ Engine::Engine(int device) {
     cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking);
     cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking);
     cudaEventCreateWithFlags(&copy_ev_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&suffix_ev_, cudaEventDisableTiming);
     cudaMallocHost((void**)&h_status_, sizeof(uint32_t));
     cudaMalloc((void**)&status_, sizeof(uint32_t));
     cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_);
@@ -134,6 +135,7 @@ Engine::~Engine() {
     if (h_status_) cudaFreeHost(h_status_);
     if (h_params_) cudaFreeHost(h_params_);
     if (copy_ev_) cudaEventDestroy(copy_ev_);
+    if (suffix_ev_) cudaEventDestroy(suffix_ev_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -598,6 +600,7 @@ int Engine::step(uint32_t substeps, bool sync) {
     int rc = prepare();
     if (rc) return rc;
     const bool graph = use_graph_ && !profiling_;
+    eager_prefix_ = false;
     for (uint32_t s = 0; s < substeps; ++s) {
         if (graph) {
             if (!prefix_valid_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
@@ -629,8 +632,29 @@ int Engine::step(uint32_t substeps, bool sync) {
     }
     for (auto& s : scenes_) s.pending = scene_defers(s);
     stepped_ = true;
-    if (sync) return read_status();
-    return ENG_OK;
+    if (!sync) return ENG_OK;
+    if (graph && scenes_.size() == 1 && !debug_) {
+        // A blocking step of a single system: read this step's status, then
+        // launch the next substep's prefix, which the next step() or a state
+        // read needs, and return once the status has arrived.  The GPU runs the
+        // prefix while the caller takes the result.  Status bits the prefix
+        // raises are read by the next call.  (Engines of many scenes, whose
+        // layout changes between steps, compute it on demand instead, and so
+        // does a system with debug taps, whose taps show the substep just run.)
+        ENG_CK(cudaMemcpyAsync(h_status_, status_, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "status read");
+        ENG_CK(cudaEventRecord(suffix_ev_, stream_), "step event");
+        ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+        prefix_valid_ = true;
+        eager_prefix_ = true;
+        ENG_CK(cudaEventSynchronize(suffix_ev_), "step sync");
+        if (*h_status_) {
+            prefix_valid_ = false;
+            eager_prefix_ = false;
+            return read_status();   // waits for the prefix, reports and clears the bits
+        }
+        return ENG_OK;
+    }
+    return read_status();
 }
 
 // Run the next substep's prefix once, for reads of scenes whose XSPH update
@@ -641,6 +665,7 @@ int Engine::step(uint32_t substeps, bool sync) {
 int Engine::ensure_prefix(bool wait) {
     if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
     if (prefix_valid_) return ENG_OK;
+    eager_prefix_ = false;
     int rc = prepare();
     if (rc) return rc;
     if (use_graph_ && !profiling_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
@@ -841,6 +866,29 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     float* dp = pos ? st : nullptr;
     float* dc = colour ? st + (size_t)n * 3 : nullptr;
     float* dv = vel ? st + (size_t)n * 6 : nullptr;
+    if (eager_prefix_ && prefix_valid_ && !layout_dirty_ && !params_dirty_) {
+        // The last blocking step left the next prefix running behind
+        // suffix_ev_: the state it ended with (P0; V0 when no update is
+        // pending) is packed and copied on the copy stream meanwhile, and a
+        // pending update's velocities follow the prefix on the main stream.
+        ENG_CK(cudaStreamWaitEvent(copy_stream_, suffix_ev_, 0), "export wait");
+        ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, pend ? nullptr : dv,
+                           copy_stream_), "pack");
+        if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
+        if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
+        if (vel && !pend) ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
+        if (pend) {
+            const StepArgs a = args();
+            ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, dv, nullptr, false, stream_),
+                   "unsort");
+            ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+        }
+        const cudaError_t ce = cudaStreamSynchronize(copy_stream_);
+        if (ce != cudaSuccess) return cuda_fail(ce, "download sync");
+        rc = read_status();   // the prefix's status; waits for the main stream too
+        if (rc) { prefix_valid_ = false; eager_prefix_ = false; return rc; }
+        return ENG_OK;
+    }
     ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, pend ? nullptr : dv, stream_),
            "pack");
     if (!pend) {

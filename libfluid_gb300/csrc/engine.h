@@ -156,6 +156,7 @@ private:
     cudaStream_t stream_ = nullptr;
     cudaStream_t copy_stream_ = nullptr;   // exports: copies that overlap the prefix
     cudaEvent_t copy_ev_ = nullptr;
+    cudaEvent_t suffix_ev_ = nullptr;      // the last blocking step's suffix (and status read) done
     std::string err_;
     std::vector<Scene> scenes_;
     int next_id_ = 1;
@@ -198,6 +199,7 @@ private:
     bool all_defer_ = false;           // every scene defers: no XSPH pass in the substep
     uint64_t pend_cap_ = 0;
     bool prefix_valid_ = false;        // the next substep's prefix has run (for a state read)
+    bool eager_prefix_ = false;        // that prefix was launched by step() behind suffix_ev_
     cudaGraph_t graph_pre_ = nullptr, graph_suf_ = nullptr;
     cudaGraphExec_t exec_pre_ = nullptr, exec_suf_ = nullptr;
     cudaEvent_t ev_[kPasses + 1] = {};

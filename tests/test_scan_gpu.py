@@ -45,6 +45,7 @@ def test_scan_many_tiles(dims, n):
     pos = (np.stack([cx, cy, cz], 1).astype(np.float64) + 0.5) * h
     pos = pos.astype(np.float32)
     fs = FluidSystem(0)
+    fs.debugEnable(True)   # the sort fields then describe the substep just run
     fs.init(n, 1)
     fs.setDomain(dims[0] * h, dims[1] * h, dims[2] * h, h)
     fs.setParams(mass=2e-4, particle_size=0.0025, dt=1e-5)
