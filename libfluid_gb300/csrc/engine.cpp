@@ -510,15 +510,25 @@ StepArgs Engine::args() const {
 // (sort and density, with any pending XSPH update) ends where a state read
 // needs it; the suffix is the rest (normals, forces and integrator, and the
 // XSPH pass of scenes that do not defer it).
-int Engine::launch_prefix(bool profile) { return launch_prefix_args(args(), profile); }
+int Engine::launch_prefix(bool profile) { return launch_prefix_args(args(), profile, !hashed_); }
 
-int Engine::launch_prefix_args(const StepArgs& a, bool profile) {
+// The hash of the current positions, for when no force pass produced it (the
+// first substep, or after the state, the layout or the parameters changed).
+int Engine::launch_hash_standalone(const StepArgs& a) {
+    ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), stream_), "memset counts");
+    ENG_CK(launch_hash(a, stream_), "hash");
+    return ENG_OK;
+}
+
+// The substep up to the density pass.  The hash normally comes from the
+// previous substep's force pass; `hash` runs it here instead (the captured
+// prefix graph never contains it).
+int Engine::launch_prefix_args(const StepArgs& a, bool profile, bool hash) {
     cudaStream_t st = stream_;
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     mark(0);
-    ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), st), "memset counts");
     ENG_CK(cudaMemsetAsync(scal_, 0, 8 * sizeof(uint32_t), st), "memset substep scalars");
-    ENG_CK(launch_hash(a, st), "hash");
+    if (hash) { int rc = launch_hash_standalone(a); if (rc) return rc; }
     mark(1);
     ENG_CK(launch_scan(a, st), "scan");
     mark(2);
@@ -535,6 +545,8 @@ int Engine::launch_suffix(bool profile) {
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     if (any_tension_) ENG_CK(launch_normals(a, st), "normals");
     mark(5);
+    // the force pass hashes its output for the next substep
+    ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), st), "memset counts");
     ENG_CK(launch_force(a, st), "force");
     mark(6);
     if (!all_defer_) ENG_CK(launch_xsph(a, st), "xsph");
@@ -547,6 +559,7 @@ int Engine::read_status() {
     ENG_CK(cudaStreamSynchronize(stream_), "step sync");
     const uint32_t st = *h_status_;
     if (st) {
+        hashed_ = false;   // hash the state afresh before the next substep
         ENG_CK(cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_), "status reset");
         if (st & SPH_STATUS_CELL_OVERFLOW)
             return fail(ENG_ECELL, "a grid cell held more than 8192 particles");
@@ -558,6 +571,7 @@ int Engine::read_status() {
 
 // Layout, parameters and (in graph mode) the two captured graphs up to date.
 int Engine::prepare() {
+    if (layout_dirty_ || params_dirty_) hashed_ = false;
     if (layout_dirty_) { int rc = rebuild_layout(); if (rc) return rc; }
     if (params_dirty_) { int rc = upload_params(); if (rc) return rc; }
     const bool graph = use_graph_ && !profiling_;
@@ -569,7 +583,7 @@ int Engine::prepare() {
             cudaGraph_t& gref = half == 0 ? graph_pre_ : graph_suf_;
             cudaGraphExec_t& eref = half == 0 ? exec_pre_ : exec_suf_;
             ENG_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
-            int rc = half == 0 ? launch_prefix(false) : launch_suffix(false);
+            int rc = half == 0 ? launch_prefix_args(args(), false, false) : launch_suffix(false);
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(stream_, &g);
             if (rc) { if (g) cudaGraphDestroy(g); return rc; }
@@ -603,7 +617,10 @@ int Engine::step(uint32_t substeps, bool sync) {
     eager_prefix_ = false;
     for (uint32_t s = 0; s < substeps; ++s) {
         if (graph) {
-            if (!prefix_valid_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+            if (!prefix_valid_) {
+                if (!hashed_) { rc = launch_hash_standalone(args()); if (rc) return rc; }
+                ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+            }
             ENG_CK(cudaGraphLaunch(exec_suf_, stream_), "graph launch");
         } else if (profiling_) {
             // a prefix computed for a state read is recomputed (same values) so
@@ -629,6 +646,7 @@ int Engine::step(uint32_t substeps, bool sync) {
             if (rc) return rc;
         }
         prefix_valid_ = false;
+        hashed_ = true;
     }
     for (auto& s : scenes_) s.pending = scene_defers(s);
     stepped_ = true;
@@ -668,8 +686,10 @@ int Engine::ensure_prefix(bool wait) {
     eager_prefix_ = false;
     int rc = prepare();
     if (rc) return rc;
-    if (use_graph_ && !profiling_) ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
-    else { rc = launch_prefix(false); if (rc) return rc; }
+    if (use_graph_ && !profiling_) {
+        if (!hashed_) { rc = launch_hash_standalone(args()); if (rc) return rc; }
+        ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+    } else { rc = launch_prefix(false); if (rc) return rc; }
     if (wait) {
         rc = read_status();
         if (rc) return rc;
@@ -690,7 +710,7 @@ int Engine::prefix_scene(const Scene& sc, bool wait) {
     a.ntiles = sc.tile_count;
     a.grid_nbr = sc.tile_count;
     a.tile_ctr = nullptr;
-    rc = launch_prefix_args(a, false);
+    rc = launch_prefix_args(a, false, !hashed_);
     if (rc) return rc;
     prefix_valid_ = false;
     return wait ? read_status() : ENG_OK;
@@ -763,6 +783,7 @@ int Engine::get_pass_times(double* ms_out, int cap, uint64_t* launches) {
 
 void Engine::clear_pending(Scene& s) {
     s.pending = false;
+    hashed_ = false;
     if (!layout_dirty_ && pend_ && s.table_index < pend_cap_) cudaMemsetAsync(pend_ + s.table_index, 0, sizeof(uint32_t), stream_);
     prefix_valid_ = false;
 }
@@ -807,6 +828,7 @@ int Engine::set_positions(int id, uint32_t first, const float* pos, uint32_t cou
     // the other particles keep their velocities: apply a pending XSPH update first
     if (s->pending) { int rc = materialize(*s); if (rc) return rc; }
     prefix_valid_ = false;
+    hashed_ = false;
     const size_t bytes = (size_t)count * 3 * sizeof(float);
     float* st = nullptr;
     int rc = staging(bytes, &st);
@@ -825,6 +847,7 @@ int Engine::generate_lattice(int id, const LatticeSpec& spec, uint32_t first) {
     if (first + n > s->n) return fail(ENG_EINVAL, "lattice exceeds the scene's particle count");
     if (s->pending) { int rc = materialize(*s); if (rc) return rc; }
     prefix_valid_ = false;
+    hashed_ = false;
     ENG_CK(launch_lattice(spec, s->part_base + first, P0_, V0_, A0_, S_, stream_), "lattice");
     return ENG_OK;
 }
@@ -985,8 +1008,7 @@ int Engine::debug_get(int id, int field, void* host, uint64_t count) {
             if (!need(n)) return fail(ENG_EINVAL, "buffer too small");
             uint32_t* tmp = nullptr;
             ENG_CK(cudaMalloc((void**)&tmp, n * sizeof(uint32_t)), "debug alloc");
-            ENG_CK(launch_sorted_keys(key_ + 0, perm_, n, pb, nc, tmp, stream_), "sorted keys");
-            // keys are indexed by global slot; launch_sorted_keys reads key[perm[base+i]]
+            ENG_CK(launch_sorted_keys(d_params_ + s->table_index, P1_, n, pb, tmp, stream_), "sorted keys");
             ENG_CK(cudaMemcpyAsync(host, tmp, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream_), "debug copy");
             ENG_CK(cudaStreamSynchronize(stream_), "debug sync");
             cudaFree(tmp);

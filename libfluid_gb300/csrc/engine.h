@@ -131,8 +131,9 @@ private:
     int ensure_capacity(uint64_t parts, uint64_t cells);
     int rebuild_layout();
     int upload_params();
-    int launch_prefix(bool profile);   // memsets, hash, scan, sort, density
-    int launch_prefix_args(const StepArgs& a, bool profile);
+    int launch_prefix(bool profile);   // [memset, hash], scan, sort, density
+    int launch_prefix_args(const StepArgs& a, bool profile, bool hash);
+    int launch_hash_standalone(const StepArgs& a);
     int prefix_scene(const Scene& s, bool wait = true);  // the prefix over one scene's tiles
     int launch_suffix(bool profile);   // normals, force + integrator, [XSPH]
     int ensure_prefix(bool wait = true);   // the next substep's prefix, computed once
@@ -200,6 +201,8 @@ private:
     uint64_t pend_cap_ = 0;
     bool prefix_valid_ = false;        // the next substep's prefix has run (for a state read)
     bool eager_prefix_ = false;        // that prefix was launched by step() behind suffix_ev_
+    bool hashed_ = false;              // key, slot and cell counts describe the current P0 (the
+                                       // last force pass hashed its output); else the prefix hashes
     cudaGraph_t graph_pre_ = nullptr, graph_suf_ = nullptr;
     cudaGraphExec_t exec_pre_ = nullptr, exec_suf_ = nullptr;
     cudaEvent_t ev_[kPasses + 1] = {};

@@ -1,7 +1,8 @@
 // sm_103a kernels of the WCSPH substep.
 //
 // One substep (the body of FluidSystem::advance, fluidsystem.cu:301-398) is:
-//   memset counts -> k_hash -> scan (3 kernels) -> k_scatter -> k_rank_gather
+//   [k_hash: only when no force pass hashed the state] -> scan (one pass)
+//   -> k_scatter -> k_rank_gather
 //   -> k_density (+ the previous substep's XSPH update) -> [k_normals]
 //   -> k_force_integrate [-> k_xsph, for scenes that do not defer XSPH]
 // Every kernel is scene-aware: a launch covers the tiles of all live scenes,
@@ -667,7 +668,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
 // fluidintegrator.cu:11-70).  Reads cell-order state (P1, the velocities Vc
 // of the density pass (V1 with any pending XSPH update applied) through the
 // V1 argument, A1, S, N), writes the integrated state to P0 (w = density), V2,
-// A0, and each particle's cell to okey.  The integrator sums the
+// A0, each particle's cell to okey, and the next substep's hash of the new
+// positions (key, slot, cell counts), so that substep needs no hash pass.
+// The integrator sums the
 // force buffers in the reference's order, which after the swapped arguments
 // at fluidsystem.cu:352-364 is ((pressure + tension) + viscosity) + adhesion.
 // ---------------------------------------------------------------------------
@@ -691,6 +694,8 @@ k_force_integrate(const DevParams* __restrict__ params,
                                                               float4* __restrict__ P0, float4* __restrict__ V2,
                                                               float4* __restrict__ A0, uint32_t* __restrict__ maxdisp,
                                                               uint32_t* __restrict__ okey, uint32_t* __restrict__ pend,
+                                                              uint32_t* __restrict__ count, uint32_t* __restrict__ key,
+                                                              uint32_t* __restrict__ slot, uint32_t* __restrict__ status,
                                                               float4* __restrict__ dbg_forces, uint32_t ntiles,
                                                               uint32_t* __restrict__ tile_ctr) {
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
@@ -830,7 +835,28 @@ k_force_integrate(const DevParams* __restrict__ params,
     P0[k] = make_float4(px, py, pz, si.x);
     V2[k] = make_float4(vx, vy, vz, 0.f);
     A0[k] = make_float4(anx, any, anz, 0.f);
-    okey[k] = grid_inside(pp, g) ? pack_cell(g) : SPH_OKEY_NULL;   // the cell XSPH's cell lists use
+    // The next substep's hash (k_hash's work, on the position just written):
+    // its cell key, a provisional slot from the cell count (made stable by
+    // the rank pass) and the non-finite check.  The cell XSPH's cell lists
+    // use is recorded with SPH_OKEY_MOVED when the particle leaves it.
+    const int3 gn = grid_of(pp, px, py, pz);
+    const bool inside_new = grid_inside(pp, gn);
+    if (!(isfinite(px) && isfinite(py) && isfinite(pz))) atomicOr(status, SPH_STATUS_NONFINITE);
+    const uint32_t local = inside_new ? (uint32_t)gn.x + (uint32_t)gn.y * pp.gx + (uint32_t)gn.z * pp.gxy : pp.ncells;
+    {
+        const uint32_t gkey = sc.cell_base + local;
+        const unsigned lane = threadIdx.x & 31u;
+        const unsigned peers = __match_any_sync(lanes, gkey);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)lane == leader) base = atomicAdd(&count[gkey], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        key[k] = local;
+        slot[k] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+    }
+    okey[k] = grid_inside(pp, g)
+                  ? (pack_cell(g) | ((inside_new && pack_cell(gn) == pack_cell(g)) ? 0u : SPH_OKEY_MOVED))
+                  : SPH_OKEY_NULL;
     // largest displacement of the substep in units of h (squared), for XSPH's
     // use of the neighbour masks; NaN compares above every finite value
     const float ddx = px - pi.x, ddy = py - pi.y, ddz = pz - pi.z;
@@ -1019,12 +1045,16 @@ __global__ void k_lattice(LatticeSpec spec, uint32_t base, float4* __restrict__ 
 
 // Sorted hash for the debug tap: key of the particle now at each slot, with
 // the NULL bucket reported as NULL_HASH (m_Hash after the sort).
-__global__ void k_sorted_keys(const uint32_t* __restrict__ key, const uint32_t* __restrict__ perm, uint32_t n,
-                              uint32_t base, uint32_t ncells, uint32_t* __restrict__ out) {
+__global__ void k_sorted_keys(const DevParams* __restrict__ params, const float4* __restrict__ P1, uint32_t n,
+                              uint32_t base, uint32_t* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const uint32_t k = key[perm[base + i]];
-    out[i] = (k == ncells) ? SPH_NULL_HASH : k;
+    // the cell of the position gathered into slot i by the last sort: the key
+    // it was sorted by (the key array itself may already hold the next
+    // substep's keys, written by the force pass)
+    const float4 p = P1[base + i];
+    const uint32_t k = cell_of(*params, p.x, p.y, p.z);
+    out[i] = (k == params->ncells) ? SPH_NULL_HASH : k;
 }
 
 // ---------------------------------------------------------------------------
@@ -1118,7 +1148,7 @@ cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
     const size_t smem = table ? (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t) : 0;
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.Vc, a.A1, a.S, a.N, a.mask,
                                             a.mask_stride, a.P0, a.V2, a.A0, a.skin_masks ? a.maxdisp : nullptr,
-                                            a.okey, a.pend, a.dbg_forces,
+                                            a.okey, a.pend, a.count, a.key, a.slot, a.status, a.dbg_forces,
                                             a.ntiles, ctr(a, 2));
     return cudaGetLastError();
 }
@@ -1152,10 +1182,10 @@ cudaError_t launch_lattice(const LatticeSpec& spec, uint32_t base, float4* P0, f
     k_lattice<<<(n + 255) / 256, 256, 0, st>>>(spec, base, P0, V0, A0, S);
     return cudaGetLastError();
 }
-cudaError_t launch_sorted_keys(const uint32_t* key, const uint32_t* perm, uint32_t n, uint32_t base,
-                               uint32_t ncells, uint32_t* out, cudaStream_t st) {
+cudaError_t launch_sorted_keys(const DevParams* params, const float4* P1, uint32_t n, uint32_t base,
+                               uint32_t* out, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_sorted_keys<<<(n + 255) / 256, 256, 0, st>>>(key, perm, n, base, ncells, out);
+    k_sorted_keys<<<(n + 255) / 256, 256, 0, st>>>(params, P1, n, base, out);
     return cudaGetLastError();
 }
 

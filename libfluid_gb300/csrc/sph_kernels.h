@@ -71,7 +71,7 @@ cudaError_t launch_pack(const float4* P0, const float4* V0, uint32_t n, uint32_t
                         float* pos, float* colour, float* vel, cudaStream_t st);
 cudaError_t launch_lattice(const LatticeSpec& spec, uint32_t base, float4* P0, float4* V0, float4* A0, float4* S,
                            cudaStream_t st);
-cudaError_t launch_sorted_keys(const uint32_t* key, const uint32_t* perm, uint32_t n, uint32_t base,
-                               uint32_t ncells, uint32_t* out, cudaStream_t st);
+cudaError_t launch_sorted_keys(const DevParams* params, const float4* P1, uint32_t n, uint32_t base,
+                               uint32_t* out, cudaStream_t st);
 
 }  // namespace sph
