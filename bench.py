@@ -336,6 +336,10 @@ def run_ours(args, dist):
     kern = {k: v for k, v in per_launch.items() if k not in ("substep",) and v > 0}
     dom = max(kern, key=kern.get)
     alg_bytes = dict(ALG_BYTES)
+    if per_launch.get("hash", 0.0) < 0.05 * per_launch.get("force_integrate", 1.0):
+        # the force pass hashed its output (reads nothing more; key and slot
+        # written, 8 B) and the hash pass only cleared the substep scalars
+        alg_bytes["force_integrate"] += 8
     if per_launch.get("xsph", 0.0) < 0.05 * per_launch.get("density", 1.0):
         # deferred XSPH: the update runs inside the density pass (its reads and
         # writes: P, V, rho 28 B, V 12 B) and there is no XSPH pass
