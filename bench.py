@@ -159,7 +159,8 @@ def profile_counters(kernel: str, workload: str):
     the neighbour passes are bound by instruction issue and gather latency,
     which the HBM fraction alone does not show."""
     path = os.path.join(ROOT, "profiles", f"counters_{workload}.txt")
-    keys = ("issue_active_pct", "lanes_per_inst", "fma_pipe_pct", "alu_pipe_pct", "dram_pct")
+    keys = ("issue_active_pct", "lanes_per_inst", "fma_pipe_pct", "alu_pipe_pct", "dram_pct", "l1tex_pct",
+            "lts_pct")
     try:
         for line in open(path):
             p = line.split()
