@@ -339,6 +339,10 @@ typedef struct sph_server_stats {
     uint64_t live_particles;
     uint64_t device_bytes;      /* arena footprint */
     uint64_t peak_live_particles;
+    double admit_seconds;       /* creating admitted scenes (initial state upload or lattice) */
+    double read_seconds;        /* reading finished scenes back and removing them */
+    double layout_seconds;      /* host work of membership changes (tile tables, parameters), part of busy */
+    uint64_t admit_retries;     /* admissions put back because the arena had no room yet */
 } sph_server_stats;
 int sph_server_create(sph_server** out, const sph_server_config* cfg);
 /* Stops the loop (running scenes are abandoned) and frees everything. */

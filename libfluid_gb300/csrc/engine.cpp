@@ -2,6 +2,7 @@
 #include "engine.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -180,7 +181,19 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
     }
     if (parts > pcap_) {
         uint64_t np = std::max<uint64_t>(parts, pcap_ + pcap_ / 2);
-        if (byte_limit_ && np * bytes_per_particle() + std::max(cells, ccap_) * 8 > byte_limit_) np = parts;
+        if (byte_limit_ && np * bytes_per_particle() + std::max(cells, ccap_) * 8 > byte_limit_) {
+            // Near the limit, grow once to what it allows (keeping 1/32 of it
+            // for cell growth), not to exactly `parts`: growing copies every
+            // per-slot array, and a server admitting scene after scene would
+            // otherwise copy the whole arena for each of them.
+            const uint64_t cell_bytes = std::max(cells, ccap_) * 8 + byte_limit_ / 32;
+            const uint64_t room = byte_limit_ > cell_bytes ? (byte_limit_ - cell_bytes) / bytes_per_particle() : 0;
+            np = std::max(parts, std::min(np, room));
+            // and never again by a sliver: a large arena that cannot grow by
+            // an eighth waits for scenes to leave instead of being copied
+            if (pcap_ >= (1u << 20) && np < pcap_ + pcap_ / 8)
+                return fail(ENG_ENOMEM, "arena at its memory budget");
+        }
         if (np >= (1ull << 31)) return fail(ENG_ENOMEM, "particle capacity exceeds 2^31");
         // state between substeps: P0, V0, A0, S, and for scenes with a
         // pending XSPH update their post-integration velocities V2 and cells
@@ -239,7 +252,10 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
     }
     if (cells > ccap_) {
         uint64_t nc = std::max<uint64_t>(cells, ccap_ + ccap_ / 2);
-        if (byte_limit_ && pcap_ * bytes_per_particle() + nc * 8 > byte_limit_) nc = cells;
+        if (byte_limit_ && pcap_ * bytes_per_particle() + nc * 8 > byte_limit_) {
+            const uint64_t used = pcap_ * bytes_per_particle();
+            nc = std::max(cells, std::min(nc, byte_limit_ > used ? (byte_limit_ - used) / 8 : 0));
+        }
         if (count_) cudaFree(count_);
         if (start_) cudaFree(start_);
         if (scan_sums_) cudaFree(scan_sums_);
@@ -571,6 +587,14 @@ int Engine::read_status() {
 
 // Layout, parameters and (in graph mode) the two captured graphs up to date.
 int Engine::prepare() {
+    if (!layout_dirty_ && !params_dirty_ && !graph_dirty_ && exec_pre_ && exec_suf_) return ENG_OK;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = prepare_work();
+    prep_seconds_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int Engine::prepare_work() {
     if (layout_dirty_ || params_dirty_) hashed_ = false;
     if (layout_dirty_) { int rc = rebuild_layout(); if (rc) return rc; }
     if (params_dirty_) { int rc = upload_params(); if (rc) return rc; }

@@ -105,6 +105,7 @@ public:
     const ExecConfig& exec() const { return exec_; }
     int sm_count() const { return sm_count_; }
     cudaStream_t stream() const { return stream_; }
+    double prep_seconds() const { return prep_seconds_; }
     const std::string& last_error() const { return err_; }
     int device() const { return device_; }
 
@@ -124,6 +125,8 @@ public:
     uint64_t device_bytes() const { return dev_bytes_; }
     // Cap on the arena footprint (0 = none): growth beyond it fails with ENG_ENOMEM.
     void set_byte_limit(uint64_t bytes) { byte_limit_ = bytes; }
+    // Grow the arenas to at least this many particle slots and cells now.
+    int reserve(uint64_t parts, uint64_t cells) { return ensure_capacity(parts, cells); }
 
 private:
     int fail(int code, const std::string& msg);
@@ -145,8 +148,10 @@ private:
         return defer_xsph_ && !debug_ && s.dp.gx <= SPH_OKEY_MAX_DIM && s.dp.gy <= SPH_OKEY_MAX_DIM &&
                s.dp.gz <= SPH_OKEY_MAX_DIM;
     }
-    int prepare();                     // layout, params and graphs up to date
+    int prepare();
+    int prepare_work();                     // layout, params and graphs up to date
     int read_status();
+    double prep_seconds_ = 0.0;        // host time spent in prepare() (layout, parameters, graphs)
     void free_all();
     uint32_t alloc_slots(uint32_t n);
     void free_slots(uint32_t base, uint32_t n);

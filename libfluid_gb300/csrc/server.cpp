@@ -106,12 +106,14 @@ void sph_server::loop() {
             }
         }
         // create admitted scenes (engine calls only on this thread)
+        const double ta0 = now();
         for (size_t ai = 0; ai < admit.size(); ++ai) {
             Request* r = admit[ai];
             int rc = eng->add_scene(r->cfg, r->n, &r->scene);
             if (rc == sph::ENG_ENOMEM && !live.empty()) {
                 // the arena is fragmented or full: wait for running scenes to leave
                 std::lock_guard<std::mutex> lk(mu);
+                st.admit_retries += admit.size() - ai;
                 for (size_t b = admit.size(); b-- > ai;) {
                     used_bytes -= admit[b]->bytes;
                     queue.push_front(admit[b]);
@@ -142,6 +144,10 @@ void sph_server::loop() {
             r->t_admit = now();
             st.admitted++;
             live.push_back(r);
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            st.admit_seconds += now() - ta0;
         }
         if (live.empty()) continue;
         uint32_t k = per_iter;
@@ -176,6 +182,7 @@ void sph_server::loop() {
         }
         // Read every finished scene before removing any: the first read runs
         // the next substep's prefix (deferred XSPH) and the others reuse it.
+        const double tr0 = now();
         std::vector<int> got(finished.size());
         for (size_t fi = 0; fi < finished.size(); ++fi) {
             Request* r = finished[fi];
@@ -198,6 +205,11 @@ void sph_server::loop() {
             }
             live.erase(std::find(live.begin(), live.end(), r));
         }
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            st.read_seconds += now() - tr0;
+            st.layout_seconds = eng->prep_seconds();
+        }
         if (!finished.empty()) cv_done.notify_all();
     }
 }
@@ -217,6 +229,11 @@ int sph_server_create(sph_server** out, const sph_server_config* cfg) {
     // membership changes nearly every iteration: launch eagerly
     s->eng->set_use_graph(false);
     s->eng->set_byte_limit(cfg->memory_budget);
+    // Cells for 1/16 of the budget up front: the cell count follows the live
+    // scenes up and down, and regrowing the cell arrays near the budget
+    // would reallocate them again and again (best effort: growth on demand
+    // remains).
+    s->eng->reserve(0, cfg->memory_budget / 16 / Engine::bytes_per_cell());
     s->th = std::thread([s] { s->loop(); });
     *out = s;
     return SPH_OK;

@@ -29,7 +29,8 @@ class ServerStats(C.Structure):
                 ("failed", C.c_uint64), ("rejected", C.c_uint64), ("iterations", C.c_uint64),
                 ("particle_steps", C.c_uint64), ("busy_seconds", C.c_double), ("live_scenes", C.c_uint32),
                 ("queued", C.c_uint32), ("live_particles", C.c_uint64), ("device_bytes", C.c_uint64),
-                ("peak_live_particles", C.c_uint64)]
+                ("peak_live_particles", C.c_uint64), ("admit_seconds", C.c_double), ("read_seconds", C.c_double),
+                ("layout_seconds", C.c_double), ("admit_retries", C.c_uint64)]
 
 
 class Server:
