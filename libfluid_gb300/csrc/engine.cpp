@@ -506,6 +506,7 @@ StepArgs Engine::args() const {
     a.V2 = V2_; a.S = S_; a.N = N_;
     a.Vc = Vc_; a.okey = okey_; a.okey1 = okey1_; a.pend = pend_;
     a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
+    a.scan_zeroes_counts = 1u;
     a.key = key_; a.slot = slot_; a.tmp = tmp_; a.perm = perm_;
     a.status = status_;
     a.mask = mask_;
@@ -561,8 +562,8 @@ int Engine::launch_suffix(bool profile) {
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     if (any_tension_) ENG_CK(launch_normals(a, st), "normals");
     mark(5);
-    // the force pass hashes its output for the next substep
-    ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), st), "memset counts");
+    // the force pass hashes its output for the next substep, adding into the
+    // counts that this substep's scan left at zero
     ENG_CK(launch_force(a, st), "force");
     mark(6);
     if (!all_defer_) ENG_CK(launch_xsph(a, st), "xsph");
@@ -688,6 +689,7 @@ int Engine::step(uint32_t substeps, bool sync) {
         ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
         prefix_valid_ = true;
         eager_prefix_ = true;
+        hashed_ = false;   // the prefix's scan consumed the counts
         ENG_CK(cudaEventSynchronize(suffix_ev_), "step sync");
         if (*h_status_) {
             prefix_valid_ = false;
@@ -714,6 +716,9 @@ int Engine::ensure_prefix(bool wait) {
         if (!hashed_) { rc = launch_hash_standalone(args()); if (rc) return rc; }
         ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
     } else { rc = launch_prefix(false); if (rc) return rc; }
+    // The scan consumed the counts: a prefix that runs again before the next
+    // force pass (a parameter change, a profiled substep) hashes afresh.
+    hashed_ = false;
     if (wait) {
         rc = read_status();
         if (rc) return rc;
@@ -734,6 +739,7 @@ int Engine::prefix_scene(const Scene& sc, bool wait) {
     a.ntiles = sc.tile_count;
     a.grid_nbr = sc.tile_count;
     a.tile_ctr = nullptr;
+    a.scan_zeroes_counts = 0u;   // keep the counts for the full prefix that follows
     rc = launch_prefix_args(a, false, !hashed_);
     if (rc) return rc;
     prefix_valid_ = false;

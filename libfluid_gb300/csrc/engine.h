@@ -207,7 +207,8 @@ private:
     bool prefix_valid_ = false;        // the next substep's prefix has run (for a state read)
     bool eager_prefix_ = false;        // that prefix was launched by step() behind suffix_ev_
     bool hashed_ = false;              // key, slot and cell counts describe the current P0 (the
-                                       // last force pass hashed its output); else the prefix hashes
+                                       // last force pass hashed its output and no full prefix's scan
+                                       // has consumed the counts since); else the prefix hashes
     cudaGraph_t graph_pre_ = nullptr, graph_suf_ = nullptr;
     cudaGraphExec_t exec_pre_ = nullptr, exec_suf_ = nullptr;
     cudaEvent_t ev_[kPasses + 1] = {};

@@ -177,6 +177,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
 // blocks start, so every tile waited on belongs to a block that is already
 // running and waits only on tiles before it; the waits are bounded all the
 // same (SPH_STATUS_SCAN_TIMEOUT, the outputs are then invalid).
+//
+// With `zero` set the kernel also leaves every count it read at zero: the
+// next substep's hash (fused into the force pass) adds into them, which
+// otherwise needs a memset of the whole count array.
 constexpr unsigned long long SCAN_AGG = 1ull << 32;
 constexpr unsigned long long SCAN_PRE = 2ull << 32;
 constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;
@@ -190,10 +194,10 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(const uint32_t* __restrict__ in, uint32_t n,
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* __restrict__ in, uint32_t n,
                                                               unsigned long long* __restrict__ desc,
                                                               uint32_t* __restrict__ out,
-                                                              uint32_t* __restrict__ status) {
+                                                              uint32_t* __restrict__ status, uint32_t zero) {
     __shared__ uint32_t s_tile, s_prefix, s_total;
     __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
     if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(desc), 1u);
@@ -202,16 +206,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(const uint32_t* __
     const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     const bool whole = base + SCAN_ITEMS <= n;   // 16 counts, 64-byte aligned
     uint32_t v[SCAN_ITEMS];
+    // each count is read (and, with `zero`, cleared at the end) by this thread alone
     if (whole) {
         const uint4* p4 = reinterpret_cast<const uint4*>(in + base);
 #pragma unroll
         for (int q = 0; q < SCAN_ITEMS / 4; ++q) {
-            const uint4 w = __ldg(p4 + q);
+            const uint4 w = p4[q];
             v[4 * q] = w.x; v[4 * q + 1] = w.y; v[4 * q + 2] = w.z; v[4 * q + 3] = w.w;
         }
     } else {
 #pragma unroll
-        for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (base + k < n) ? __ldg(in + base + k) : 0u;
+        for (int k = 0; k < SCAN_ITEMS; ++k) v[k] = (base + k < n) ? in[base + k] : 0u;
     }
     uint32_t s = 0;
 #pragma unroll
@@ -278,6 +283,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(const uint32_t* __
             o4[q] = w;
         }
         if (base + SCAN_ITEMS == n) out[n] = run;   // total after the last cell
+        if (zero) {
+            uint4* z4 = reinterpret_cast<uint4*>(in + base);
+#pragma unroll
+            for (int q = 0; q < SCAN_ITEMS / 4; ++q) z4[q] = make_uint4(0u, 0u, 0u, 0u);
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < SCAN_ITEMS; ++k) {
@@ -285,6 +295,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(const uint32_t* __
             if (idx < n) out[idx] = run;
             run += v[k];
             if (idx + 1 == n) out[n] = run;
+            if (zero && idx < n) in[idx] = 0u;
         }
     }
 }
@@ -1095,7 +1106,7 @@ cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
     unsigned long long* desc = reinterpret_cast<unsigned long long*>(a.scan_sums);
     cudaError_t e = cudaMemsetAsync(desc, 0, (size_t)(nt + 1) * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, desc, a.start, a.status);
+    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, desc, a.start, a.status, a.scan_zeroes_counts);
     return cudaGetLastError();
 }
 cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,

@@ -22,6 +22,7 @@ struct StepArgs {
     float4 *S;                 // (rho, p, c^2, 0)
     float4 *N;                 // normals
     uint32_t *count, *start, *scan_sums;
+    uint32_t scan_zeroes_counts;   // nonzero: the scan leaves every count it read at zero for the next hash
     uint32_t *key, *slot, *tmp, *perm;
     uint32_t *status;
     uint32_t *mask;            // SPH_MASK_ROWS neighbour-mask words per slot, word m at mask[m*mask_stride + slot]:
