@@ -95,3 +95,49 @@ def test_batch_join_and_param_change_with_pending_updates():
     b.close()
     for x, y in zip(got, want):
         assert np.array_equal(x, y)
+
+
+def test_reads_then_profiled_or_partial_prefixes_keep_the_run():
+    """A full prefix's scan clears the cell counts that the force pass built;
+    a prefix run again before the next force pass (profiled substeps after a
+    read) must hash afresh, and a read of one scene of a batch (a prefix over
+    that scene's tiles) must leave the counts for the full prefix.  Neither
+    may change the trajectory."""
+    spec = W.small_dam_break(seed=35)
+    want = _plain(spec, 7)
+    fs = configure_gpu(FluidSystem(0), spec)
+    for _ in range(2):
+        fs.advance(spec.dt, 1)
+        fs.exportToData()                # the next prefix has run
+    fs.setProfiling(True)                # profiled substeps recompute that prefix
+    for _ in range(3):
+        fs.advance(spec.dt, 1)
+    fs.setProfiling(False)
+    fs.exportToData()
+    for _ in range(2):
+        fs.advance(spec.dt, 1)
+    got = fs.exportToData()
+    fs.close()
+    for x, y in zip(got, want):
+        assert np.array_equal(x, y)
+
+    specs = W.batch_manifest(num_scenes=2, seed=45, nmin=2000, nmax=6000)
+
+    def run(mid_reads):
+        b = Batch(0)
+        ids = [b.add_scene(s) for s in specs]
+        for k in range(5):
+            b.step(1)
+            if mid_reads and k in (1, 3):
+                b.get_state(ids[1])      # a prefix over scene 1's tiles only
+            if mid_reads and k == 3:
+                b.set_profiling(True)
+        b.set_profiling(False)
+        out = [b.get_state(i) for i in ids]
+        b.close()
+        return out
+
+    plain, read = run(False), run(True)
+    for sa, sb in zip(plain, read):
+        for x, y in zip(sa, sb):
+            assert np.array_equal(x, y)
