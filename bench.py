@@ -207,6 +207,9 @@ def workload(name: str):
         return W.dam_break_1m(unit_cube=True), "1M dam break in the reference's unit cube (res 100, h=0.01 m)"
     if name == "small_dam_break":
         return W.small_dam_break(), "32,768-particle dam break in a 1.0x0.6x0.6 m box, h=0.02 m, dt=2e-4 s"
+    if name == "small_dam_break_cube":
+        return (W.small_dam_break(unit_cube=True),
+                "32,768-particle dam break in the reference's unit cube (res 50, h=0.02 m)")
     if name == "large_tension":
         return W.large_tension(), ("8,005,232 particles with surface tension 0.0728: 200x200x180 lattice pool plus "
                                    "falling spheres, h=0.01 m, dt=8e-5 s")
@@ -262,7 +265,8 @@ def reference_cuda_compare(args, fs):
     from oracle import ref_cuda
     if not ref_cuda.available():
         return {"unavailable": "oracle/_ref/libfluid_ref.cubin not built (needs the reference sources)"}
-    spec, desc = workload("dam_break_1m_cube")
+    # the unit-cube form of the workload measured (the reference has no other domain)
+    spec, desc = workload("small_dam_break_cube" if args.workload == "small_dam_break" else "dam_break_1m_cube")
     pos, vel = spec.positions(), spec.velocities()
     p = spec.params()
     rp = dict(p)

@@ -384,7 +384,8 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // candidates are not scanned in phase 1; phase 2 walks them in full with the
 // test.  Both phases visit candidates in the reference's order, so the sum is
 // the candidate-order sum.  WALK selects phase 1's loop: flattened across the
-// rows (0) or one loop per row with four loads in flight (1); the words are
+// rows (0) or one loop per row with four candidates in flight, two per
+// 256-bit load (1); the words are
 // the same.
 //
 // Deferred XSPH.  For a scene whose previous substep ended without its XSPH
@@ -399,6 +400,15 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // corrected velocity goes to Vc, which the force pass reads; without a
 // pending update Vc = V1.
 // ---------------------------------------------------------------------------
+// Two consecutive cell-ordered positions in one 256-bit load: the slot must
+// be even (32-byte aligned from the 256-byte aligned arena).  The positions
+// are not written during the pass that reads them.
+__device__ __forceinline__ void ld_pos_pair(const float4* p, float4& a, float4& b) {
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+}
+
 #ifndef DENSITY_MINB
 #define DENSITY_MINB 4
 #endif
@@ -487,9 +497,16 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                 const uint32_t ce = min(cb + 32u, je0);
                 uint32_t dm = 0u, sm = 0u, bit = 1u;
                 uint32_t jj = cb;
+                // from an even slot on, two candidates per 256-bit load
+                if ((jj & 1u) != 0u) {
+                    visit(__ldg(P1 + jj), bit, dm, sm);
+                    bit <<= 1;
+                    ++jj;
+                }
                 for (; jj + 4u <= ce; jj += 4u) {
-                    const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
-                    const float4 q2 = __ldg(P1 + jj + 2u), q3 = __ldg(P1 + jj + 3u);
+                    float4 q0, q1, q2, q3;
+                    ld_pos_pair(P1 + jj, q0, q1);
+                    ld_pos_pair(P1 + jj + 2u, q2, q3);
                     visit(q0, bit, dm, sm);
                     visit(q1, bit << 1, dm, sm);
                     visit(q2, bit << 2, dm, sm);
@@ -497,7 +514,8 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                     bit <<= 4;
                 }
                 if (jj + 2u <= ce) {
-                    const float4 q0 = __ldg(P1 + jj), q1 = __ldg(P1 + jj + 1u);
+                    float4 q0, q1;
+                    ld_pos_pair(P1 + jj, q0, q1);
                     visit(q0, bit, dm, sm);
                     visit(q1, bit << 1, dm, sm);
                     bit <<= 2;

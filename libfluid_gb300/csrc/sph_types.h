@@ -66,7 +66,7 @@ struct DevParams {
 // Kernel variants (bits of the execution config's `variant`). All variants
 // visit neighbours in the same order and give identical results; they differ
 // only in how the walk is scheduled.
-#define SPH_VARIANT_DENSITY_ROWS  0x1u   // density: one loop per cell row, four loads in flight
+#define SPH_VARIANT_DENSITY_ROWS  0x1u   // density: one loop per cell row, four candidates in flight (two 256-bit loads)
 #define SPH_VARIANT_XSPH_ROWS     0x2u   // XSPH: one loop per cell row instead of one flattened walk
 #define SPH_VARIANT_FORCE_OCC     0x4u   // force: 64-register build (more resident warps)
 #define SPH_VARIANT_FORCE_TABLE   0x8u   // force: walk over a per-thread row table in shared memory
