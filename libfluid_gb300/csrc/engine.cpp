@@ -99,7 +99,7 @@ bool derive_params(const SceneConfig& c, DevParams& d, std::string* err) {
     return true;
 }
 
-uint64_t Engine::bytes_per_particle() { return 10 * 16 + 6 * 4 + SPH_MASK_ROWS * 4; }
+uint64_t Engine::bytes_per_particle() { return 10 * 16 + 5 * 4 + SPH_MASK_ROWS * 4; }
 uint64_t Engine::bytes_per_cell() { return 2 * 4 + 1; }
 const char* Engine::pass_name(int i) { return (i >= 0 && i < kPasses) ? kPassNames[i] : "?"; }
 
@@ -159,7 +159,7 @@ void Engine::free_all() {
     float4** f4[] = {&P0_, &P1_, &V0_, &V1_, &V2_, &A0_, &A1_, &S_, &N_, &Vc_, &dbg_forces_};
     for (auto p : f4) { if (*p) cudaFree(*p); *p = nullptr; }
     uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &count_, &start_, &scan_sums_, &dbg_nbr_, &mask_,
-                      &okey_, &okey1_, &pend_};
+                      &okey_, &pend_};
     for (auto p : u) { if (*p) cudaFree(*p); *p = nullptr; }
     if (stage_) cudaFree(stage_);
     stage_ = nullptr;
@@ -228,7 +228,7 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
             cudaError_t e = cudaMalloc((void**)p, np * sizeof(float4));
             if (e != cudaSuccess) return fail(ENG_ENOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
         }
-        uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_, &okey1_};
+        uint32_t** u[] = {&key_, &slot_, &tmp_, &perm_};
         for (auto p : u) {
             if (*p) cudaFree(*p);
             *p = nullptr;
@@ -504,7 +504,7 @@ StepArgs Engine::args() const {
     a.P0 = P0_; a.V0 = V0_; a.A0 = A0_;
     a.P1 = P1_; a.V1 = V1_; a.A1 = A1_;
     a.V2 = V2_; a.S = S_; a.N = N_;
-    a.Vc = Vc_; a.okey = okey_; a.okey1 = okey1_; a.pend = pend_;
+    a.Vc = Vc_; a.okey = okey_; a.pend = pend_;
     a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
     a.scan_zeroes_counts = 1u;
     a.key = key_; a.slot = slot_; a.tmp = tmp_; a.perm = perm_;

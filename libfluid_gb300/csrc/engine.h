@@ -172,7 +172,7 @@ private:
     // device arenas
     float4 *P0_ = nullptr, *P1_ = nullptr, *V0_ = nullptr, *V1_ = nullptr, *V2_ = nullptr, *A0_ = nullptr,
            *A1_ = nullptr, *S_ = nullptr, *N_ = nullptr, *Vc_ = nullptr;
-    uint32_t *okey_ = nullptr, *okey1_ = nullptr;   // packed cells: last substep (state), gathered
+    uint32_t *okey_ = nullptr;         // packed cells of the last substep (state order)
     uint32_t *pend_ = nullptr;                      // per scene-table entry: XSPH update pending
     uint32_t *key_ = nullptr, *slot_ = nullptr, *tmp_ = nullptr, *perm_ = nullptr;
     uint32_t *count_ = nullptr, *start_ = nullptr, *scan_sums_ = nullptr, *status_ = nullptr;

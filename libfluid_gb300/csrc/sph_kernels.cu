@@ -12,7 +12,8 @@
 //   P0,V0,A0  state between substeps (P0.w = density of the last substep)
 //   V2, okey  post-integration velocity and cell of the last substep, for a
 //             scene whose XSPH update is pending (pend[scene] != 0)
-//   P1,V1,A1  state gathered into cell order (okey1: the gathered cells)
+//   P1,V1,A1  state gathered into cell order (with a pending update, V1.w
+//             holds the gathered okey bits)
 //   S         (rho, p, c^2, 1/rho^2) per sorted slot
 //   Vc        cell-ordered velocities with the pending XSPH update applied
 //   N         surface normals (only when a scene has surface tension)
@@ -340,7 +341,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
                                                           const uint32_t* __restrict__ okey,
                                                           const uint32_t* __restrict__ pend,
                                                           float4* __restrict__ P1, float4* __restrict__ V1,
-                                                          float4* __restrict__ A1, uint32_t* __restrict__ okey1,
+                                                          float4* __restrict__ A1,
                                                           uint32_t* __restrict__ perm,
                                                           uint32_t* __restrict__ status) {
     const uint4 t = tiles[blockIdx.x];
@@ -362,9 +363,12 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
     const uint32_t f = b + rank;
     perm[f] = i;
     P1[f] = P0[i];
-    V1[f] = pending ? V2[i] : V0[i];
+    float4 v = pending ? V2[i] : V0[i];
+    // the cell of the last substep travels with the velocity (w lane) to the
+    // density pass's XSPH update, which loads both together
+    if (pending) v.w = __uint_as_float(__ldg(okey + i));
+    V1[f] = v;
     A1[f] = A0[i];
-    if (pending) okey1[f] = __ldg(okey + i);
 }
 
 // ---------------------------------------------------------------------------
@@ -390,8 +394,8 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 //
 // Deferred XSPH.  For a scene whose previous substep ended without its XSPH
 // update (pend[scene] != 0), P1 holds that substep's post-integration
-// positions (w = its densities), V1 its post-integration velocities and okey1
-// the cells the particles were sorted into then.  The reference's update
+// positions (w = its densities), V1 its post-integration velocities with, in
+// the w lane, the cells the particles were sorted into then (okey bits).  The reference's update
 // (correctVelocityXSPH, fluidphysics.cu:355-409) sums over pairs with
 // r^2 <= h^2 at these positions whose previous cells are adjacent (its cell
 // lists were those of the previous sort); every such pair is within h now, so
@@ -420,7 +424,6 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                                                       const float4* __restrict__ P1, float4* __restrict__ S,
                                                       uint32_t* __restrict__ mask, size_t mask_stride,
                                                       const float4* __restrict__ V1,
-                                                      const uint32_t* __restrict__ okey1,
                                                       const uint32_t* __restrict__ pend, float4* __restrict__ Vc,
                                                       uint32_t* __restrict__ nbr_out, uint32_t ntiles,
                                                       uint32_t* __restrict__ tile_ctr) {
@@ -435,7 +438,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     const int3 g = grid_of(pp, p.x, p.y, p.z);
     if (!grid_inside(pp, g)) {
         S[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        Vc[k] = vi;
+        Vc[k] = make_float4(vi.x, vi.y, vi.z, 0.f);
         if (nbr_out) nbr_out[k] = 0;
         return;
     }
@@ -574,21 +577,19 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     float sum = 0.0f;
     uint32_t cnt = 0;
     // deferred XSPH of the previous substep (only for particles that had a cell then)
-    const uint32_t oi = (__ldg(pend + t.x) != 0u) ? __ldg(okey1 + k) : SPH_OKEY_NULL;
+    const uint32_t oi = (__ldg(pend + t.x) != 0u) ? __float_as_uint(vi.w) : SPH_OKEY_NULL;
     const bool xs = oi != SPH_OKEY_NULL;
     float ax = 0.f, ay = 0.f, az = 0.f;
     TableWalk walk(tab, ts, live, full);
     uint32_t j;
     while (walk.next(j)) {
-        // the pair's XSPH operands are loaded with its position, before any
-        // test, so that the three latencies overlap
+        // the pair's XSPH operands (velocity, and its last cell in the w
+        // lane) are loaded with its position, before any test, so that the
+        // two latencies overlap
         const float4 q = __ldg(P1 + j);
         float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
-        uint32_t oj = SPH_OKEY_NULL;
-        if (xs) {
-            vj = __ldg(V1 + j);
-            oj = __ldg(okey1 + j);
-        }
+        if (xs) vj = __ldg(V1 + j);
+        const uint32_t oj = __float_as_uint(vj.w);
         const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
         // true for every recorded bit; the test matters in rows walked in full
@@ -618,7 +619,8 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     const float cs = pp.gas_constant * powf(ratio, pp.gamma - 1.0f);
     // w = 1/rho^2, used by the force pass for p_j/rho_i^2 + p_i/rho_j^2
     S[k] = make_float4(rho, prs, cs, 1.0f / (rho * rho));
-    Vc[k] = xs ? make_float4(fmaf(pp.xsph, ax, vi.x), fmaf(pp.xsph, ay, vi.y), fmaf(pp.xsph, az, vi.z), 0.f) : vi;
+    Vc[k] = xs ? make_float4(fmaf(pp.xsph, ax, vi.x), fmaf(pp.xsph, ay, vi.y), fmaf(pp.xsph, az, vi.z), 0.f)
+               : make_float4(vi.x, vi.y, vi.z, 0.f);
     if (nbr_out) nbr_out[k] = cnt;
   });
 }
@@ -1139,7 +1141,7 @@ cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_s
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
     k_scatter<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
     k_rank_gather<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.V2,
-                                                a.okey, a.pend, a.P1, a.V1, a.A1, a.okey1, a.perm, a.status);
+                                                a.okey, a.pend, a.P1, a.V1, a.A1, a.perm, a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
@@ -1148,7 +1150,7 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
                              : (rows ? k_density<1, false> : k_density<0, false>);
     const size_t smem = (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t);   // the row table
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
-                                            a.V1, a.okey1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
+                                            a.V1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
     return cudaGetLastError();
 }
 cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,

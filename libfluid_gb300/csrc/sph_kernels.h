@@ -17,7 +17,7 @@ struct StepArgs {
     float4 *P1, *V1, *A1;      // cell-ordered state
     float4 *V2;                // post-integration velocity (before XSPH)
     float4 *Vc;                // cell-ordered velocities with any pending XSPH update applied
-    uint32_t *okey, *okey1;    // each slot's cell in the last substep (packed), and gathered into cell order
+    uint32_t *okey;            // each slot's cell in the last substep (packed; gathered into V1.w)
     uint32_t *pend;            // per scene: its last XSPH update is pending
     float4 *S;                 // (rho, p, c^2, 0)
     float4 *N;                 // normals
