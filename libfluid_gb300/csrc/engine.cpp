@@ -1,6 +1,8 @@
 // Host-side engine (see engine.h).
 #include "engine.h"
 
+#include "arena_policy.h"
+
 #include <algorithm>
 #include <chrono>
 #include <cfloat>
@@ -175,25 +177,12 @@ void Engine::free_all() {
 // Grow the particle and cell arenas, preserving live particle state.
 int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
     cudaSetDevice(device_);
-    if (byte_limit_) {
-        const uint64_t need = std::max(parts, pcap_) * bytes_per_particle() + std::max(cells, ccap_) * 8;
-        if (need > byte_limit_) return fail(ENG_ENOMEM, "arena would exceed the memory budget");
-    }
-    if (parts > pcap_) {
-        uint64_t np = std::max<uint64_t>(parts, pcap_ + pcap_ / 2);
-        if (byte_limit_ && np * bytes_per_particle() + std::max(cells, ccap_) * 8 > byte_limit_) {
-            // Near the limit, grow once to what it allows (keeping 1/32 of it
-            // for cell growth), not to exactly `parts`: growing copies every
-            // per-slot array, and a server admitting scene after scene would
-            // otherwise copy the whole arena for each of them.
-            const uint64_t cell_bytes = std::max(cells, ccap_) * 8 + byte_limit_ / 32;
-            const uint64_t room = byte_limit_ > cell_bytes ? (byte_limit_ - cell_bytes) / bytes_per_particle() : 0;
-            np = std::max(parts, std::min(np, room));
-            // and never again by a sliver: a large arena that cannot grow by
-            // an eighth waits for scenes to leave instead of being copied
-            if (pcap_ >= (1u << 20) && np < pcap_ + pcap_ / 8)
-                return fail(ENG_ENOMEM, "arena at its memory budget");
-        }
+    // sizes under the memory budget (arena_policy.h)
+    const ArenaPlan plan = plan_arena(parts, cells, pcap_, ccap_, byte_limit_, bytes_per_particle());
+    if (plan.status == kArenaOverBudget) return fail(ENG_ENOMEM, "arena would exceed the memory budget");
+    if (plan.status == kArenaAtBudget) return fail(ENG_ENOMEM, "arena at its memory budget");
+    if (plan.parts > pcap_) {
+        const uint64_t np = plan.parts;
         if (np >= (1ull << 31)) return fail(ENG_ENOMEM, "particle capacity exceeds 2^31");
         // state between substeps: P0, V0, A0, S, and for scenes with a
         // pending XSPH update their post-integration velocities V2 and cells
@@ -250,12 +239,8 @@ int Engine::ensure_capacity(uint64_t parts, uint64_t cells) {
         pcap_ = np;
         graph_dirty_ = true;
     }
-    if (cells > ccap_) {
-        uint64_t nc = std::max<uint64_t>(cells, ccap_ + ccap_ / 2);
-        if (byte_limit_ && pcap_ * bytes_per_particle() + nc * 8 > byte_limit_) {
-            const uint64_t used = pcap_ * bytes_per_particle();
-            nc = std::max(cells, std::min(nc, byte_limit_ > used ? (byte_limit_ - used) / 8 : 0));
-        }
+    if (plan.cells > ccap_) {
+        const uint64_t nc = plan.cells;
         if (count_) cudaFree(count_);
         if (start_) cudaFree(start_);
         if (scan_sums_) cudaFree(scan_sums_);
