@@ -29,6 +29,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -88,11 +89,11 @@ class ClockSampler:
          "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
          "clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu: int):
+    def __init__(self, gpu: int, path: str | None = None):
         self.gpu = gpu
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_gpu{gpu}.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else f"/tmp/sph_clocks_{os.getpid()}_{gpu}.csv"
+        # the raw samples: where --clocks-csv says, else a temporary file
+        self.path = path or os.path.join(tempfile.gettempdir(), f"sph_clocks_{os.getpid()}_{gpu}.csv")
 
     def start(self):
         try:
@@ -312,7 +313,7 @@ def run_ours(args, dist):
     fs.sync()
 
     # ---- timed region: K substeps as CUDA-graph replays, state resident ----
-    clocks = ClockSampler(dist.local)
+    clocks = ClockSampler(dist.local, args.clocks_csv)
     clocks.start()
     dist.barrier()
     fs.sync()
@@ -444,7 +445,7 @@ def run_batched(args, dist):
     # the plain comparison covers the first k_plain substeps of the timed
     # region (the scenes get more expensive as they compress)
     k_plain = max(3, min(args.steps, 50))
-    clocks = ClockSampler(dist.local)
+    clocks = ClockSampler(dist.local, args.clocks_csv)
     clocks.start()
     b.sync()
     b.timer_mark(0)
@@ -590,6 +591,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-refcuda", action="store_true")
+    ap.add_argument("--clocks-csv", default=None,
+                    help="keep the nvidia-smi clock samples of the timed region in this CSV file")
     ap.add_argument("--tile", type=int, default=None, choices=[64, 128, 256],
                     help="plain workload: particles per tile (threads per block; default: the compiled default)")
     ap.add_argument("--variant", type=int, default=None,
