@@ -434,6 +434,8 @@ def run_batched(args, dist):
     from libfluid_gb300.batch import Batch
     from libfluid_gb300 import autotune
     specs = W.batch_manifest(num_scenes=args.scenes, seed=7)
+    if args.manifest and dist.rank == 0:
+        write_manifest(args.manifest, W.manifest(specs, workload="batched", seed=7))
     exe = autotune.load("batched") or {}
     b = Batch(dist.local)
     b.set_exec(**exe)
@@ -494,6 +496,12 @@ def run_batched(args, dist):
         print(json.dumps(line), flush=True)
 
 
+def write_manifest(path: str, m: dict) -> None:
+    """The workload's scenes (and arrival times) as JSON (workloads.manifest)."""
+    with open(path, "w") as f:
+        json.dump(m, f)
+
+
 def served_requests(count: int, seed: int):
     """Requests of the served workload: dam breaks as in the batched set but
     with particles log-uniform in [1,024, 262,144] and substeps uniform in
@@ -510,6 +518,7 @@ def run_served(args, dist):
     (arrival to final state on the host) and aggregate particle-steps/s,
     against the plain sequential step on the same requests."""
     import threading
+    from libfluid_gb300 import workloads as W
     from libfluid_gb300.batch import Batch
     from libfluid_gb300.server import Server
     specs, steps = served_requests(args.requests, seed=13)
@@ -535,9 +544,13 @@ def run_served(args, dist):
     plain_rate = sample_work / (plain_ms * 1e-3)
     results = []
     rng = np.random.default_rng(99)
-    for rate in args.rates:
+    all_gaps = [rng.exponential(1.0 / rate, size=len(specs)) for rate in args.rates]
+    if args.manifest and dist.rank == 0:
+        arrivals = {str(rate): np.cumsum(g).tolist() for rate, g in zip(args.rates, all_gaps)}
+        write_manifest(args.manifest, W.manifest(specs, steps, workload="served", seed=13,
+                                                 arrival_seconds_per_rate=arrivals))
+    for rate, gaps in zip(args.rates, all_gaps):
         srv = Server(dist.local, memory_budget=100 << 30)
-        gaps = rng.exponential(1.0 / rate, size=len(specs))
         ids = [None] * len(specs)
         t0 = time.perf_counter()
 
@@ -591,6 +604,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-refcuda", action="store_true")
+    ap.add_argument("--manifest", default=None,
+                    help="batched/served workloads: write their scenes (and arrival times) to this JSON file")
     ap.add_argument("--clocks-csv", default=None,
                     help="keep the nvidia-smi clock samples of the timed region in this CSV file")
     ap.add_argument("--tile", type=int, default=None, choices=[64, 128, 256],

@@ -210,3 +210,40 @@ def batch_manifest(num_scenes: int = 256, seed: int = 7, nmin: int = 2048, nmax:
                              particle_size=0.5 * spacing, viscosity=float(rng.uniform(0.005, 0.05)),
                              surface_tension=float(rng.uniform(0.0, 0.07)), dt=2e-4, steps=steps))
     return out
+
+
+def manifest(specs: list, steps: list | None = None, **extra) -> dict:
+    """A JSON-ready record of a scene set: per scene its particle count,
+    domain, parameters, fluid blocks (with their seeds) and substeps, so that
+    a run can be inspected or replayed without the generator that drew it
+    (`from_manifest`).  `extra` entries (workload name, seed, arrival times)
+    are stored beside the scenes."""
+    scenes = []
+    for k, s in enumerate(specs):
+        if s.extra_pos is not None:
+            raise ValueError("a scene with host-generated particles has no manifest form")
+        blocks = []
+        for b in s.blocks:
+            d = dataclasses.asdict(b)
+            blocks.append({key: (list(v) if isinstance(v, tuple) else v) for key, v in d.items()})
+        params = {key: (list(v) if isinstance(v, tuple) else v) for key, v in s.params().items()}
+        scenes.append({"n": s.n, "box": list(s.box), "h": s.h, "unit_cube_res": s.unit_cube_res,
+                       "boundary": s.boundary, "params": params, "blocks": blocks,
+                       "steps": int(steps[k]) if steps is not None else int(s.steps)})
+    out = {"scenes": scenes, "total_particles": sum(sc["n"] for sc in scenes)}
+    out.update(extra)
+    return out
+
+
+def from_manifest(m: dict) -> tuple[list, list]:
+    """The scenes and substep counts of a `manifest` record."""
+    specs, steps = [], []
+    for sc in m["scenes"]:
+        p = dict(sc["params"])
+        p["gravity"] = tuple(p["gravity"])
+        blocks = [Lattice(**{k: (tuple(v) if isinstance(v, list) else v) for k, v in b.items()})
+                  for b in sc["blocks"]]
+        specs.append(SceneSpec(box=tuple(sc["box"]), h=sc["h"], blocks=blocks, steps=sc["steps"],
+                               unit_cube_res=sc["unit_cube_res"], boundary=sc["boundary"], **p))
+        steps.append(sc["steps"])
+    return specs, steps
