@@ -138,10 +138,19 @@ def _extra_signatures():
     return _capi_batch.SIGNATURES
 
 
+# what a failure without a handle to ask (a failed create) means
+_NO_HANDLE_MSG = {
+    SPH_ECUDA: "no CUDA device is visible or the CUDA runtime failed; the library has no CPU path",
+    SPH_EINVAL: "invalid argument (for a create: a device index out of range or an invalid configuration)",
+}
+
+
 def check(code: int, handle=None) -> None:
     if code != SPH_OK:
         msg = ""
         if handle is not None:
             raw = lib().sph_last_error(handle)
             msg = raw.decode() if raw else ""
+        else:
+            msg = _NO_HANDLE_MSG.get(code, "")
         raise SphError(code, msg)

@@ -5,7 +5,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._capi import SphError, SphParams, lib
+from ._capi import SphError, SphParams, check, lib
 from ._capi_batch import SphLattice
 from .batch import lattice_struct, params_struct
 from .workloads import SceneSpec
@@ -41,9 +41,7 @@ class Server:
         self._L = lib()
         cfg = ServerConfig(device, memory_budget, max_live_scenes, substeps_per_iteration)
         h = C.c_void_p()
-        rc = self._L.sph_server_create(C.byref(h), C.byref(cfg))
-        if rc != 0:
-            raise SphError(rc, "server create failed")
+        check(self._L.sph_server_create(C.byref(h), C.byref(cfg)))
         self._h = h
         self._n: dict[int, int] = {}
 
