@@ -15,6 +15,13 @@ inputs.  A step is one WCSPH substep of that scene (advance(dt, 1)).
              of positions, colours, velocities to the host).
   cpu_baseline  the CPU oracle (OpenMP restatement of the reference step)
              on a bounded sample of the same scene, on this host's cores.
+  batched    256 mixed-size dam breaks (2,048-65,536 particles) advanced by
+             one launch per pass for 200 substeps, against the same scenes
+             stepped one at a time over the same substeps.
+  served     1,000 requests (1,024-262,144 particles, 50-500 substeps) under
+             open-loop Poisson arrivals at 50, 100 and 2,000 requests/s:
+             p50/p99 latency and aggregate particle-steps/s, against the
+             plain sequential step.
 
 --impl reference times the reference's step on host cores (the oracle port:
 the reference has no CPU implementation of its own and its CUDA sources do
@@ -403,6 +410,12 @@ def run_ours(args, dist):
     if not args.skip_refcuda and dist.world == 1:
         refcuda = reference_cuda_compare(args, fs)
 
+    # ---- the two systems forms, on their own workloads (rank 0 at N=1) ----
+    batched = served = None
+    if not args.skip_systems and dist.world == 1:
+        batched = measure_batched(dist, args.scenes, args.batched_steps, 3)
+        served = measure_served(dist, args.served_requests, args.served_rates)
+
     # the one-pass scan, scatter, rank+gather, density, force+integrate (which
     # also hashes the next substep) (+ normals with surface tension, + the
     # XSPH pass when it is not deferred into the next density pass); the
@@ -418,6 +431,7 @@ def run_ours(args, dist):
                        "parallelism": "replicas" if dist.world > 1 else "single GPU",
                        "timing": "CUDA events on the library stream, graph replay"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "reference_cuda": refcuda,
+            "batched": batched, "served": served,
             "gpu_launches": launches_per_substep * args.steps, "clocks": clk,
             "passes_ms_per_substep": per_launch,
             "published_reference": {"value": 7.7e7, "unit": "particle-steps/s",
@@ -427,71 +441,77 @@ def run_ours(args, dist):
         print(json.dumps(line), flush=True)
 
 
-def run_batched(args, dist):
-    """256 mixed-size dam breaks (2,048-65,536 particles each) advanced by one
-    launch per pass, against the plain step run one scene at a time."""
+BATCH_DESC = ("dam-break scenes, particles log-uniform [2048, 65536], aspect [0.5,2], box 2x/1.2x the block, "
+              "visc U[0.005,0.05], tension U[0,0.07], spacing 0.01 m, h 0.02 m, dt 2e-4 s")
+
+
+def measure_batched(dist, num_scenes: int, steps: int, warmup: int, clocks_csv=None, manifest=None) -> dict:
+    """Mixed-size dam breaks (2,048-65,536 particles each) advanced by one
+    launch per pass, against the plain step run one scene at a time over the
+    same substeps (each scene alone after the same warm-up)."""
     from libfluid_gb300 import workloads as W
     from libfluid_gb300.batch import Batch
     from libfluid_gb300 import autotune
-    specs = W.batch_manifest(num_scenes=args.scenes, seed=7)
-    if args.manifest and dist.rank == 0:
-        write_manifest(args.manifest, W.manifest(specs, workload="batched", seed=7))
+    specs = W.batch_manifest(num_scenes=num_scenes, seed=7)
+    if manifest and dist.rank == 0:
+        write_manifest(manifest, W.manifest(specs, workload="batched", seed=7))
     exe = autotune.load("batched") or {}
     b = Batch(dist.local)
     b.set_exec(**exe)
     for s in specs:
         b.add_scene(s)
     total_n = sum(s.n for s in specs)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.step(1)
-    # the plain comparison covers the first k_plain substeps of the timed
-    # region (the scenes get more expensive as they compress)
-    k_plain = max(3, min(args.steps, 50))
-    clocks = ClockSampler(dist.local, args.clocks_csv)
+    clocks = ClockSampler(dist.local, clocks_csv)
     clocks.start()
     b.sync()
     b.timer_mark(0)
-    for i in range(args.steps):
+    for _ in range(steps):
         b.step_async(1)
-        if i + 1 == k_plain:
-            b.timer_mark(2)
     b.timer_mark(1)
     ms = b.timer_elapsed(0, 1)
-    ms_first = b.timer_elapsed(0, 2)
     b.sync()
     clk = clocks.stop()
-    value = total_n * args.steps / (ms * 1e-3)
-    value_first = total_n * k_plain / (ms_first * 1e-3)
+    value = total_n * steps / (ms * 1e-3)
     b.close()
-    # plain step, one scene at a time (each scene its own engine, graph replay)
+    # the plain step, one scene at a time: each scene in its own engine, the
+    # same warm-up, then the same substeps timed (graph replay)
     plain_ms = 0.0
     for s in specs:
         one = Batch(dist.local)
         one.set_exec(**exe)
         one.add_scene(s)
-        for _ in range(3):
+        for _ in range(warmup):
             one.step(1)
         one.sync()
         one.timer_mark(0)
-        for _ in range(k_plain):
+        for _ in range(steps):
             one.step_async(1)
         one.timer_mark(1)
         plain_ms += one.timer_elapsed(0, 1)
         one.close()
-    plain = total_n * k_plain / (plain_ms * 1e-3)
-    line = {"metric": METRIC, "workload": "batched", "value": value, "unit": "particle-steps/s",
-            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+    plain = total_n * steps / (plain_ms * 1e-3)
+    return {"value": value, "unit": "particle-steps/s", "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+            "scenes": len(specs), "particles": total_n,
+            "workload": f"{len(specs)} {BATCH_DESC}",
+            "timing": "CUDA events, graph replay, one launch per pass",
+            "exec": exe or "engine defaults",
+            "plain_one_at_a_time": {"value": plain, "steps": steps, "warmup": warmup,
+                                    "how": "each scene alone in its own engine, the same warm-up and the same "
+                                           "substeps, graph replay, summed device time"},
+            "speedup_vs_plain": value / plain, "clocks": clk}
+
+
+def run_batched(args, dist):
+    r = measure_batched(dist, args.scenes, args.steps, args.warmup, args.clocks_csv, args.manifest)
+    line = {"metric": METRIC, "workload": "batched", "value": r["value"], "unit": "particle-steps/s",
+            "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"{len(specs)} dam-break scenes, particles log-uniform [2048, 65536], aspect "
-                                   "[0.5,2], box 2x/1.2x the block, visc U[0.005,0.05], tension U[0,0.07], "
-                                   "spacing 0.01 m, h 0.02 m, dt 2e-4 s", "scenes": len(specs),
-                       "particles": total_n, "timing": "CUDA events, graph replay, one launch per pass",
-                       "exec": exe or "engine defaults"},
-            "plain_one_at_a_time": {"value": plain, "steps": k_plain,
-                                    "how": "each scene alone in its own engine, graph replay, summed device time"},
-            "batched_same_substeps": {"value": value_first, "steps": k_plain,
-                                      "how": "the batch's first k substeps of the timed region"},
-            "speedup_vs_plain": value_first / plain, "clocks": clk}
+            "config": {"workload": r["workload"], "scenes": r["scenes"], "particles": r["particles"],
+                       "timing": r["timing"], "exec": r["exec"]},
+            "plain_one_at_a_time": r["plain_one_at_a_time"], "speedup_vs_plain": r["speedup_vs_plain"],
+            "clocks": r["clocks"]}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -513,20 +533,20 @@ def served_requests(count: int, seed: int):
     return specs, [int(x) for x in steps]
 
 
-def run_served(args, dist):
-    """Open-loop Poisson arrivals at each rate of --rates; p50/p99 latency
-    (arrival to final state on the host) and aggregate particle-steps/s,
-    against the plain sequential step on the same requests."""
+def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: int = 64) -> dict:
+    """Open-loop Poisson arrivals at each rate; p50/p99 latency (arrival to
+    final state on the host) and aggregate particle-steps/s, against the
+    plain sequential step on the same requests."""
     import threading
     from libfluid_gb300 import workloads as W
     from libfluid_gb300.batch import Batch
     from libfluid_gb300.server import Server
-    specs, steps = served_requests(args.requests, seed=13)
+    specs, steps = served_requests(num_requests, seed=13)
     work = sum(s.n * k for s, k in zip(specs, steps))
-    # plain sequential step: per-substep device time of each request alone
-    # (graph replay), summed over its substeps
+    # plain sequential step: per-substep device time of each sampled request
+    # alone (graph replay), times its substeps
     plain_ms = 0.0
-    sample = list(range(0, len(specs), max(1, len(specs) // 64)))
+    sample = list(range(0, len(specs), max(1, len(specs) // plain_sample)))
     sample_work = 0
     for i in sample:
         one = Batch(dist.local)
@@ -544,12 +564,12 @@ def run_served(args, dist):
     plain_rate = sample_work / (plain_ms * 1e-3)
     results = []
     rng = np.random.default_rng(99)
-    all_gaps = [rng.exponential(1.0 / rate, size=len(specs)) for rate in args.rates]
-    if args.manifest and dist.rank == 0:
-        arrivals = {str(rate): np.cumsum(g).tolist() for rate, g in zip(args.rates, all_gaps)}
-        write_manifest(args.manifest, W.manifest(specs, steps, workload="served", seed=13,
-                                                 arrival_seconds_per_rate=arrivals))
-    for rate, gaps in zip(args.rates, all_gaps):
+    all_gaps = [rng.exponential(1.0 / rate, size=len(specs)) for rate in rates]
+    if manifest and dist.rank == 0:
+        arrivals = {str(rate): np.cumsum(g).tolist() for rate, g in zip(rates, all_gaps)}
+        write_manifest(manifest, W.manifest(specs, steps, workload="served", seed=13,
+                                            arrival_seconds_per_rate=arrivals))
+    for rate, gaps in zip(rates, all_gaps):
         srv = Server(dist.local, memory_budget=100 << 30)
         ids = [None] * len(specs)
         t0 = time.perf_counter()
@@ -579,17 +599,27 @@ def run_served(args, dist):
         lat = np.asarray(lat)
         results.append({"rate_req_s": rate, "requests": len(specs), "p50_s": float(np.percentile(lat, 50)),
                         "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
-                        "throughput": work / (last - first), "wall_s": wall,
-                        "busy_frac": st["busy_seconds"] / max(last - first, 1e-9),
-                        "mean_live_scenes": None, "peak_live_particles": st["peak_live_particles"]})
-    line = {"metric": METRIC, "workload": "served", "unit": "particle-steps/s", "value": max(r["throughput"] for r in results),
-            "higher_is_better": True, "n_gpus": dist.world, "dtype": "f32", "data": "synthetic",
-            "config": {"requests": len(specs), "particles": "log-uniform [1024, 262144]", "substeps": "U[50,500]",
-                       "arrivals": "open-loop Poisson", "memory_budget_bytes": 100 << 30,
-                       "offered_particle_steps": work},
+                        "throughput": work / (last - first), "offered": rate * work / len(specs),
+                        "wall_s": wall, "busy_frac": st["busy_seconds"] / max(last - first, 1e-9),
+                        "peak_live_particles": st["peak_live_particles"]})
+    best = max(r["throughput"] for r in results)
+    return {"value": best, "unit": "particle-steps/s",
+            "workload": f"{len(specs)} requests: dam breaks as in the batched set, particles log-uniform "
+                        "[1024, 262144], substeps U[50,500], open-loop Poisson arrivals, 100 GB budget",
+            "requests": len(specs), "offered_particle_steps": work,
             "plain_sequential": {"value": plain_rate, "how": f"{len(sample)} requests alone, per-substep device "
                                                              "time x their substeps"},
-            "rates": results}
+            "speedup_vs_plain": best / plain_rate, "rates": results}
+
+
+def run_served(args, dist):
+    r = measure_served(dist, args.requests, args.rates, args.manifest)
+    line = {"metric": METRIC, "workload": "served", "unit": "particle-steps/s", "value": r["value"],
+            "higher_is_better": True, "n_gpus": dist.world, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": r["workload"], "requests": r["requests"], "memory_budget_bytes": 100 << 30,
+                       "offered_particle_steps": r["offered_particle_steps"]},
+            "plain_sequential": r["plain_sequential"], "speedup_vs_plain": r["speedup_vs_plain"],
+            "rates": r["rates"]}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -612,6 +642,14 @@ def main():
                     help="plain workload: particles per tile (threads per block; default: the compiled default)")
     ap.add_argument("--variant", type=int, default=None,
                     help="plain workload: kernel variant bits (SPH_VARIANT_*; default: the compiled default)")
+    ap.add_argument("--skip-systems", action="store_true",
+                    help="plain workload: leave out the batched and served measurements")
+    ap.add_argument("--batched-steps", type=int, default=200,
+                    help="plain workload: substeps of its batched measurement")
+    ap.add_argument("--served-requests", type=int, default=1000,
+                    help="plain workload: requests of its served measurement")
+    ap.add_argument("--served-rates", type=float, nargs="+", default=[50, 100, 2000],
+                    help="plain workload: arrival rates (req/s) of its served measurement")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="served workload: number of requests")
     # the knee is near 55 req/s (mean request 1.25e7 particle-steps, ~7e8 particle-steps/s

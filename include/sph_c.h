@@ -201,6 +201,15 @@ enum sph_field {
  * sph_advance). */
 int sph_debug_enable(sph_system* s, int on);
 int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
+/* Test control of the error path of the cell scan (no counterpart: the
+ * reference's scan is thrust's, which cannot fail this way).  The scan's
+ * look-back waits give up after spin_limit polls (0: the default, 2^22)
+ * and then report SPH_ETIMEOUT.  With withhold_first_tile != 0 no block of
+ * the scan takes the first tile of cells, so every wait that reaches it
+ * runs out: the step returns SPH_ETIMEOUT, no pass after the scan touches
+ * the particles, and the state stays as it was before the failed substep.
+ * sph_debug_scan_fault(s, 0, 0) restores normal operation. */
+int sph_debug_scan_fault(sph_system* s, uint32_t spin_limit, int withhold_first_tile);
 
 /* ---- execution options and profiling ----------------------------------- */
 /* How the substep is launched (no effect on results: every choice computes
@@ -373,10 +382,13 @@ const char* sph_server_last_error(sph_server* s);
  * its scratch in a fixed 128 KiB array inside the library instead of a
  * cudaMalloc.  n must be 1..SPH_NOALLOC_MAX_CELLS, else SPH_EINVAL.
  * Enqueued on `stream` (a cudaStream_t; NULL = legacy default stream) on
- * the current device; it does not synchronise.  The first call on each
- * device looks up the scratch address (cudaGetSymbolAddress), so make that
- * first call before any stream capture.  Every call shares the scratch:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * the current device; it does not synchronise.  Each call looks up the
+ * scratch address in the current context (cudaGetSymbolAddress), so the call
+ * stays valid after the application resets the device; the first call on a
+ * device may also load the library's device code (lazy module loading), so
+ * make that first call before any stream capture.  Every call shares the
+ * scratch: calls that overlap on the GPU race and must be serialised by the
+ * caller. */
 #define SPH_NOALLOC_MAX_TILES 32768u
 #define SPH_NOALLOC_MAX_CELLS (SPH_NOALLOC_MAX_TILES * 4096u)
 int sph_scan_cells_noalloc(const uint32_t* counts, uint32_t n, uint32_t* starts, void* stream);

@@ -193,6 +193,12 @@ class FluidSystem:
     def debugEnable(self, on: bool = True) -> None:
         self._ck(self._L.sph_debug_enable(self._h, 1 if on else 0))
 
+    def debugScanFault(self, spin_limit: int = 0, withhold_first_tile: bool = False) -> None:
+        """Test control of the cell scan's bounded waits (sph_debug_scan_fault):
+        with withhold_first_tile the next substep's scan gives up after
+        spin_limit polls per wait and the step raises SPH_ETIMEOUT."""
+        self._ck(self._L.sph_debug_scan_fault(self._h, spin_limit, 1 if withhold_first_tile else 0))
+
     def debug(self, field: str, ncells: int | None = None) -> np.ndarray:
         f = FIELDS[field]
         n = self.numParticles()

@@ -98,6 +98,7 @@ SIGNATURES = [
     ("sph_get_derived", _I, [_P, C.POINTER(C.c_double), _I]),
     ("sph_derive_params", _I, [C.POINTER(SphParams), C.POINTER(C.c_double), _I]),
     ("sph_debug_enable", _I, [_P, _I]),
+    ("sph_debug_scan_fault", _I, [_P, _U32, _I]),
     ("sph_debug_get", _I, [_P, _I, _P, C.c_uint64]),
     ("sph_set_use_graph", _I, [_P, _I]),
     ("sph_set_profiling", _I, [_P, _I]),

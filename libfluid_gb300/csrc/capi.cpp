@@ -415,6 +415,11 @@ int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count) {
     if (!s->is_init || s->scene < 0) return set_err(s, SPH_ENOTINIT, "no particles");
     return eng_err(s, s->eng->debug_get(s->scene, field, buf, count));
 }
+int sph_debug_scan_fault(sph_system* s, uint32_t spin_limit, int withhold_first_tile) {
+    if (!s) return SPH_EINVAL;
+    s->eng->set_scan_fault(spin_limit, withhold_first_tile != 0);
+    return SPH_OK;
+}
 int sph_set_use_graph(sph_system* s, int on) {
     if (!s) return SPH_EINVAL;
     s->eng->set_use_graph(on != 0);

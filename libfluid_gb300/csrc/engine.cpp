@@ -426,6 +426,10 @@ int Engine::rebuild_layout() {
         any_tension_ = any_tension_ || (s.dp.flags & 1u);
         h_pend[k] = s.pending ? 1u : 0u;
     }
+    // cells are indexed with u32 (keys, starts, and the scan's tile
+    // arithmetic, which rounds up to whole 4096-cell tiles)
+    if (cb > 0xFFFFFFFFull - 2ull * kScanTileCells)
+        return fail(ENG_ENOMEM, "the live scenes need more than 2^32 - 8192 grid cells");
     total_cells_ = (uint32_t)cb;
     int rc = ensure_capacity(slots_end_, cb);
     if (rc) return rc;
@@ -492,6 +496,8 @@ StepArgs Engine::args() const {
     a.Vc = Vc_; a.okey = okey_; a.pend = pend_;
     a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
     a.scan_zeroes_counts = 1u;
+    a.scan_spin_limit = scan_spin_limit_;
+    a.scan_withhold = scan_withhold_ ? 1u : 0u;
     a.key = key_; a.slot = slot_; a.tmp = tmp_; a.perm = perm_;
     a.status = status_;
     a.mask = mask_;

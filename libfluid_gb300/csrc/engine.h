@@ -99,6 +99,17 @@ public:
     int set_deferred_xsph(bool on);
     bool deferred_xsph() const { return defer_xsph_; }
 
+    // Test control of the cell scan's look-back waits: spin_limit polls per
+    // wait (0: the default), and with `withhold` no block takes the first
+    // tile, so every wait that reaches it runs out and the step reports
+    // ENG_ETIMEOUT with the state as it was before the failed substep.
+    void set_scan_fault(uint32_t spin_limit, bool withhold) {
+        scan_spin_limit_ = spin_limit;
+        scan_withhold_ = withhold;
+        graph_dirty_ = true;
+        prefix_valid_ = false;
+    }
+
     // Options.
     void set_use_graph(bool on) { use_graph_ = on; graph_dirty_ = true; }
     int set_exec(const ExecConfig& e);
@@ -204,6 +215,8 @@ private:
     bool defer_xsph_ = true;
     bool all_defer_ = false;           // every scene defers: no XSPH pass in the substep
     uint64_t pend_cap_ = 0;
+    uint32_t scan_spin_limit_ = 0;     // set_scan_fault
+    bool scan_withhold_ = false;
     bool prefix_valid_ = false;        // the next substep's prefix has run (for a state read)
     bool eager_prefix_ = false;        // that prefix was launched by step() behind suffix_ev_
     bool hashed_ = false;              // key, slot and cell counts describe the current P0 (the

@@ -14,8 +14,12 @@
 
 namespace sph {
 
+// helper_math's dot, a.x*b.x + a.y*b.y + a.z*b.z, as the reference build
+// evaluates it: nvcc fuses the x product into the first add and the z
+// product into the second.  The order decides r^2 to the last bit, and with
+// it whether a pair at r = h counts and how large (h - r) is.
 __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
-    return fmaf(az, bz, fmaf(ay, by, ax * bx));
+    return fmaf(az, bz, fmaf(ax, bx, ay * by));
 }
 
 // Box signed distance, negative inside (boundarySDF, fluidutil.cu:85-102).

@@ -74,6 +74,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_hash(const DevParams* __restrict__
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+static_assert(SCAN_TILE == (int)kScanTileCells, "scan tile size");
 
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
     const unsigned lane = threadIdx.x & 31u;
@@ -105,9 +106,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const uint32_t* __
     }
 }
 
-// Single block: exclusive scan of up to 1024*32 tile sums, in place.
+// Single block: exclusive scan of up to kScanRawMaxTiles tile sums, in place.
 __global__ void __launch_bounds__(1024) k_scan_top(uint32_t* __restrict__ sums, uint32_t nt) {
     constexpr int ITEMS = 32;
+    static_assert(ITEMS * 1024 == (int)kScanRawMaxTiles, "k_scan_top capacity");
     uint32_t v[ITEMS];
     const uint32_t base = threadIdx.x * ITEMS;
     uint32_t s = 0;
@@ -184,7 +186,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const uint32_t* __re
 // otherwise needs a memset of the whole count array.
 constexpr unsigned long long SCAN_AGG = 1ull << 32;
 constexpr unsigned long long SCAN_PRE = 2ull << 32;
-constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;   // the default limit (StepArgs.scan_spin_limit = 0)
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
     unsigned long long v;
@@ -198,7 +200,8 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* __restrict__ in, uint32_t n,
                                                               unsigned long long* __restrict__ desc,
                                                               uint32_t* __restrict__ out,
-                                                              uint32_t* __restrict__ status, uint32_t zero) {
+                                                              uint32_t* __restrict__ status, uint32_t zero,
+                                                              uint32_t spin_limit) {
     __shared__ uint32_t s_tile, s_prefix, s_total;
     __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
     if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(desc), 1u);
@@ -248,7 +251,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* __restri
                     uint32_t spins = 0;
                     d = ld_relaxed_u64(desc + 1 + idx);
                     while ((d >> 32) == 0ull) {
-                        if (++spins > SCAN_SPIN_LIMIT) {
+                        if (++spins > spin_limit) {
                             atomicOr(status, SPH_STATUS_SCAN_TIMEOUT);
                             d = SCAN_PRE;
                             break;
@@ -301,6 +304,13 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* __restri
     }
 }
 
+// The cell starts are invalid once a wait of the scan ran out: every pass
+// that indexes with them returns at once (the whole block alike, since no
+// pass after the scan sets that bit), and the step reports SPH_ETIMEOUT.
+__device__ __forceinline__ bool scan_failed(const uint32_t* status) {
+    return (__ldcg(status) & SPH_STATUS_SCAN_TIMEOUT) != 0u;
+}
+
 // ---------------------------------------------------------------------------
 // Scatter: provisional slot of each particle in cell order.
 // ---------------------------------------------------------------------------
@@ -309,7 +319,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_scatter(const DevScene* __restrict
                                                       const uint32_t* __restrict__ start,
                                                       const uint32_t* __restrict__ key,
                                                       const uint32_t* __restrict__ slot,
-                                                      uint32_t* __restrict__ tmp) {
+                                                      uint32_t* __restrict__ tmp,
+                                                      const uint32_t* __restrict__ status) {
+    if (scan_failed(status)) return;
     const uint4 t = tiles[blockIdx.x];
     if (threadIdx.x >= t.z) return;
     const uint32_t i = t.y + threadIdx.x;
@@ -344,6 +356,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
                                                           float4* __restrict__ A1,
                                                           uint32_t* __restrict__ perm,
                                                           uint32_t* __restrict__ status) {
+    if (scan_failed(status)) return;
     const uint4 t = tiles[blockIdx.x];
     if (threadIdx.x >= t.z) return;
     const uint32_t g = t.y + threadIdx.x;
@@ -426,8 +439,10 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                                                       const float4* __restrict__ V1,
                                                       const uint32_t* __restrict__ pend, float4* __restrict__ Vc,
                                                       uint32_t* __restrict__ nbr_out, uint32_t ntiles,
-                                                      uint32_t* __restrict__ tile_ctr) {
+                                                      uint32_t* __restrict__ tile_ctr,
+                                                      const uint32_t* __restrict__ status) {
   extern __shared__ uint32_t s_rows[];
+  if (scan_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
@@ -640,7 +655,9 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
                                                       const float4* __restrict__ S,
                                                       const uint32_t* __restrict__ mask, size_t mask_stride,
                                                       float4* __restrict__ N, uint32_t ntiles,
-                                                      uint32_t* __restrict__ tile_ctr) {
+                                                      uint32_t* __restrict__ tile_ctr,
+                                                      const uint32_t* __restrict__ status) {
+  if (scan_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     const DevParams& pp = params[t.x];
     if (!(pp.flags & 1u)) return;
@@ -729,6 +746,7 @@ k_force_integrate(const DevParams* __restrict__ params,
                                                               uint32_t* __restrict__ slot, uint32_t* __restrict__ status,
                                                               float4* __restrict__ dbg_forces, uint32_t ntiles,
                                                               uint32_t* __restrict__ tile_ctr) {
+  if (scan_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     // lanes holding a particle of this tile (taken before any divergence)
     const unsigned lanes = __ballot_sync(0xffffffffu, threadIdx.x < t.z);
@@ -942,7 +960,9 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
                                                    const uint32_t* __restrict__ mask, size_t mask_stride,
                                                    const uint32_t* __restrict__ maxdisp, float4* __restrict__ V0,
                                                    uint32_t* __restrict__ pend, uint32_t ntiles,
-                                                   uint32_t* __restrict__ tile_ctr) {
+                                                   uint32_t* __restrict__ tile_ctr,
+                                                   const uint32_t* __restrict__ status) {
+  if (scan_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
@@ -1117,29 +1137,39 @@ cudaError_t init_kernel_attributes() {
     return cudaSuccess;
 }
 
-// a.scan_sums holds nt + 1 64-bit words: the tile counter, then one
-// look-back descriptor per tile; both start at zero.
+// a.scan_sums holds at least nt + 2 64-bit words: the tile counter, then one
+// look-back descriptor per tile; they start at zero.  With scan_withhold the
+// counter starts at 1 instead: the blocks take tiles 1..nt, no block takes
+// tile 0, and every wait that reaches tile 0 runs out after scan_spin_limit
+// polls (the test of the timeout path).  Tile nt covers no cell (its first
+// cell is past n), so it reads and writes no count or start, and its
+// descriptor is word nt + 1.
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
     const uint32_t n = a.total_cells;
     if (n == 0) return cudaErrorInvalidValue;
     const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
     unsigned long long* desc = reinterpret_cast<unsigned long long*>(a.scan_sums);
-    cudaError_t e = cudaMemsetAsync(desc, 0, (size_t)(nt + 1) * sizeof(unsigned long long), st);
+    cudaError_t e = cudaMemsetAsync(desc, 0, (size_t)(nt + 2) * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
-    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, desc, a.start, a.status, a.scan_zeroes_counts);
+    if (a.scan_withhold) {
+        e = cudaMemsetAsync(desc, 1, 1, st);   // the counter's low byte: the next tile handed out is 1
+        if (e != cudaSuccess) return e;
+    }
+    const uint32_t limit = a.scan_spin_limit ? a.scan_spin_limit : SCAN_SPIN_LIMIT;
+    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, desc, a.start, a.status, a.scan_zeroes_counts, limit);
     return cudaGetLastError();
 }
 cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,
                             cudaStream_t st) {
     const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
-    if (n == 0 || nt > 1024u * 32u) return cudaErrorInvalidValue;
+    if (n == 0 || nt > kScanRawMaxTiles) return cudaErrorInvalidValue;
     k_scan_reduce<<<nt, SCAN_THREADS, 0, st>>>(counts, n, tile_sums);
     k_scan_top<<<1, 1024, 0, st>>>(tile_sums, nt);
     k_scan_down<<<nt, SCAN_THREADS, 0, st>>>(counts, n, tile_sums, starts);
     return cudaGetLastError();
 }
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
-    k_scatter<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp);
+    k_scatter<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.slot, a.tmp, a.status);
     k_rank_gather<<<a.ntiles, a.block, 0, st>>>(a.scenes, a.tiles, a.start, a.key, a.tmp, a.P0, a.V0, a.A0, a.V2,
                                                 a.okey, a.pend, a.P1, a.V1, a.A1, a.perm, a.status);
     return cudaGetLastError();
@@ -1150,7 +1180,7 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
                              : (rows ? k_density<1, false> : k_density<0, false>);
     const size_t smem = (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t);   // the row table
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
-                                            a.V1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0));
+                                            a.V1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0), a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,
@@ -1165,7 +1195,7 @@ cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {
     auto kern = table ? k_normals<true> : k_normals<false>;
     const size_t smem = table ? (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t) : 0;
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
-                                            a.N, a.ntiles, ctr(a, 1));
+                                            a.N, a.ntiles, ctr(a, 1), a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
@@ -1186,7 +1216,7 @@ cudaError_t launch_force(const StepArgs& a, cudaStream_t st) {
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st) {
     auto kern = (a.variant & SPH_VARIANT_XSPH_ROWS) ? k_xsph<1> : k_xsph<0>;
     kern<<<a.grid_nbr, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.P0, a.V2, a.mask,
-                                         a.mask_stride, a.maxdisp, a.V0, a.pend, a.ntiles, ctr(a, 3));
+                                         a.mask_stride, a.maxdisp, a.V0, a.pend, a.ntiles, ctr(a, 3), a.status);
     return cudaGetLastError();
 }
 cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,

@@ -23,6 +23,8 @@ struct StepArgs {
     float4 *N;                 // normals
     uint32_t *count, *start, *scan_sums;
     uint32_t scan_zeroes_counts;   // nonzero: the scan leaves every count it read at zero for the next hash
+    uint32_t scan_spin_limit;      // polls of one look-back wait before it gives up (SPH_STATUS_SCAN_TIMEOUT)
+    uint32_t scan_withhold;        // test control: tile 0 is never handed out, so waits on it run out
     uint32_t *key, *slot, *tmp, *perm;
     uint32_t *status;
     uint32_t *mask;            // SPH_MASK_ROWS neighbour-mask words per slot, word m at mask[m*mask_stride + slot]:
@@ -50,8 +52,12 @@ cudaError_t init_kernel_attributes();
 
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st);
+// Cells per scan tile, and the most tiles launch_scan_raw takes (k_scan_top
+// scans them in one block of 1024 threads, 32 sums each).
+constexpr uint32_t kScanTileCells = 4096u;
+constexpr uint32_t kScanRawMaxTiles = 1024u * 32u;
 // Exclusive scan of counts[0,n) into starts[0,n] with caller-provided tile
-// sums (ceil(n/4096) entries, at most 32768).
+// sums (ceil(n/kScanTileCells) entries, at most kScanRawMaxTiles).
 cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,
                             cudaStream_t st);
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st);

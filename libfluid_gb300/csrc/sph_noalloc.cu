@@ -17,34 +17,28 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <mutex>
-
 #include "../../include/sph_c.h"
 #include "sph_kernels.h"
 
+static_assert(SPH_NOALLOC_MAX_TILES == sph::kScanRawMaxTiles, "scratch holds every tile sum the scan takes");
+static_assert(SPH_NOALLOC_MAX_CELLS == SPH_NOALLOC_MAX_TILES * sph::kScanTileCells, "cell limit");
+
 namespace {
 
-constexpr uint32_t kTile = 4096;                       // cells per scan tile (sph_kernels.cu)
-constexpr uint32_t kMaxTiles = SPH_NOALLOC_MAX_TILES;  // one u32 sum per tile
+static __device__ __align__(256) uint32_t g_tile_sums[SPH_NOALLOC_MAX_TILES];
 
-static __device__ __align__(256) uint32_t g_tile_sums[kMaxTiles];
-
-// Device address of g_tile_sums, looked up once per device.  In host code
-// the name g_tile_sums is only a host-side stand-in, never a device address.
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-uint32_t* g_addr[kMaxDevices] = {};
-
+// Device address of g_tile_sums in the current device's current context.  In
+// host code the name g_tile_sums is only a host-side stand-in, never a device
+// address.  It is looked up on every call rather than cached: an application
+// that calls cudaDeviceReset gets a new context, and with it a new address,
+// so a cached one could point into freed memory.  The lookup is a host-side
+// table read once the module is loaded; the first call on a device may load
+// the module (lazy loading), which is why that call should come before any
+// stream capture.
 int scratch_for_current_device(uint32_t** out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SPH_ECUDA;
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_tile_sums) != cudaSuccess || !p) return SPH_ECUDA;
-        g_addr[dev] = (uint32_t*)p;
-    }
-    *out = g_addr[dev];
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_tile_sums) != cudaSuccess || !p) return SPH_ECUDA;
+    *out = static_cast<uint32_t*>(p);
     return SPH_OK;
 }
 

@@ -18,7 +18,9 @@ PARAMS = {"rest_density": 0, "particle_size": 1, "gas_constant": 2, "xsph": 3, "
           "viscosity": 5, "adhesion": 6, "vdamp": 7, "gamma": 8, "mass": 9, "dt": 10}
 VEC_FIELDS = {"pos": 0, "vel": 1, "acc": 2, "normal": 3, "fpressure": 4, "ftension": 5, "fadhesion": 6,
               "fviscosity": 7, "colour": 8, "vel_int": 9}
-SCALAR_FIELDS = {"density": 16, "pressure": 17, "soundspeed": 18, "rho_sum": 19}
+SCALAR_FIELDS = {"density": 16, "pressure": 17, "soundspeed": 18, "rho_sum": 19,
+                 # test scales (track_scales): sum over pairs of each pair term's magnitude
+                 "fpressure_scale": 20, "fviscosity_scale": 21, "ftension_scale": 22, "normal_scale": 23}
 U32_FIELDS = {"hash_pre": 32, "hash": 33, "perm": 34, "cellstart": 35, "cellocc": 36, "nbrcount": 37}
 STAGES = {"hash_sort": 0, "density": 1, "normals": 2, "forces": 3, "integrate": 4, "xsph": 5, "colour": 6}
 
@@ -43,7 +45,7 @@ def lib() -> C.CDLL:
             "orc_substep_count": (C.c_int64, [F, U]), "orc_advance": (C.c_int64, [P, F, U]),
             "orc_stage": (C.c_int, [P, C.c_int]), "orc_num_particles": (U, [P]), "orc_num_cells": (U, [P]),
             "orc_get_params": (C.c_int, [P, P, C.c_int]), "orc_get": (C.c_int, [P, C.c_int, P, P, P, C.c_uint64]),
-            "orc_set_threads": (C.c_int, [C.c_int]),
+            "orc_set_threads": (C.c_int, [C.c_int]), "orc_track_scales": (C.c_int, [P, C.c_int]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -89,6 +91,12 @@ class Oracle:
         """0: the box (the reference's boundary); 1: the sphere of radius min
         half extent about the box centre."""
         self._ck(self._L.orc_set_boundary(self._h, shape))
+
+    def track_scales(self, on: bool = True):
+        """Also record, per particle, the sum of the magnitudes of the pair
+        terms of the pressure, viscosity and tension forces and of the normal
+        (fields *_scale): the scale of a cancelling sum's rounding error."""
+        self._ck(self._L.orc_track_scales(self._h, 1 if on else 0))
 
     def set_param(self, name: str, v: float):
         self._ck(self._L.orc_set_param(self._h, PARAMS[name], v))

@@ -74,8 +74,15 @@ template <class T> inline V3<T> operator*(V3<T> a, T s) { return mk(a.x * s, a.y
 template <class T> inline V3<T> operator*(T s, V3<T> a) { return mk(s * a.x, s * a.y, s * a.z); }
 template <class T> inline V3<T> operator/(V3<T> a, T s) { return mk(a.x / s, a.y / s, a.z / s); }
 template <class T> inline T fma_(T a, T b, T c) { return std::fma(a, b, c); }
-template <class T> inline T dot(V3<T> a, V3<T> b) { return fma_(a.z, b.z, fma_(a.y, b.y, a.x * b.x)); }
+// helper_math's dot (a.x*b.x + a.y*b.y + a.z*b.z) with the multiply-add
+// fusion of the reference's nvcc build: the x product into the first add,
+// the z product into the second (pinned by the reference-built goldens).
+template <class T> inline T dot(V3<T> a, V3<T> b) { return fma_(a.z, b.z, fma_(a.x, b.x, a.y * b.y)); }
 template <class T> inline T sqrt_(T x) { return std::sqrt(x); }
+// magnitude in double (test scales only)
+template <class T> inline double vnorm(V3<T> a) {
+    return std::sqrt(double(a.x) * double(a.x) + double(a.y) * double(a.y) + double(a.z) * double(a.z));
+}
 template <class T> inline T pow_(T x, T y) { return std::pow(x, y); }
 template <class T> inline V3<T> fmaV(V3<T> a, T s, V3<T> c) { return mk(fma_(a.x, s, c.x), fma_(a.y, s, c.y), fma_(a.z, s, c.z)); }
 template <class T> inline V3<T> fmaV(T s, V3<T> a, V3<T> c) { return mk(fma_(s, a.x, c.x), fma_(s, a.y, c.y), fma_(s, a.z, c.z)); }
@@ -299,6 +306,14 @@ template <class T> struct Sim : SimBase {
     bool isInit = false;
     std::vector<V3<T>> pos, vel, acc, nrm, fp, ft, fa, fv, colour, vint;   // vint: velocity before XSPH
     std::vector<T> rho, prs, cs, rho_sum;   // rho_sum: neighbour sum before the boundary term
+    // Test scales (only with track_scales): per particle the sum over its
+    // pairs of the magnitude of each pair's term in the pressure, viscosity
+    // and tension forces and in the normal, scaled as the result is.  A sum
+    // of cancelling terms has rounding error proportional to this, not to
+    // the net value.  Off by default so that the timed oracle does no more
+    // than the reference's arithmetic.
+    bool track_scales = false;
+    std::vector<T> sc_fp, sc_fv, sc_ft, sc_nrm;
     std::vector<uint32_t> hash_pre, hash, perm, cellOcc, cellStart, nbr;
     uint64_t substeps_done = 0;
 
@@ -316,6 +331,7 @@ template <class T> struct Sim : SimBase {
         ft = fa = fv = fp;
         colour = vint = fp;
         rho.assign(n, T(0)); prs.assign(n, T(0)); cs.assign(n, T(0)); rho_sum.assign(n, T(0));
+        sc_fp.assign(n, T(0)); sc_fv.assign(n, T(0)); sc_ft.assign(n, T(0)); sc_nrm.assign(n, T(0));
         hash_pre.assign(n, 0); hash.assign(n, 0); perm.resize(n);
         for (uint32_t i = 0; i < n; ++i) perm[i] = i;
         nbr.assign(n, 0);
@@ -425,6 +441,7 @@ template <class T> struct Sim : SimBase {
             const uint32_t i = (uint32_t)ii;
             if (hash[i] == NULL_HASH) { nrm[i] = mk(T(0), T(0), T(0)); continue; }
             V3<T> sum = mk(T(0), T(0), T(0));
+            double mag = 0.0;
             for_neighbours(hash[i], [&](uint32_t o) {
                 const V3<T> rv = pos[i] - pos[o];
                 const T r2 = dot(rv, rv);
@@ -432,9 +449,11 @@ template <class T> struct Sim : SimBase {
                     const T r = sqrt_(r2);
                     const V3<T> t = ((P.mass * grad_poly6(P, r)) * rv) / (rho[o] * r);
                     sum = sum + t;
+                    if (track_scales) mag += vnorm(t);
                 }
             });
             nrm[i] = P.h * sum;
+            if (track_scales) sc_nrm[i] = T(std::fabs(double(P.h)) * mag);
         }
     }
 
@@ -449,6 +468,7 @@ template <class T> struct Sim : SimBase {
                 continue;
             }
             V3<T> ps = mk(T(0), T(0), T(0)), vs = ps, ts = ps;
+            double mp = 0.0, mv = 0.0, mt = 0.0;   // test scales (track_scales)
             const V3<T> pi = pos[i], vi = vel[i], ni = nrm[i];
             const T ri = rho[i], pri = prs[i], csi = cs[i];
             for_neighbours(hash[i], [&](uint32_t o) {
@@ -471,12 +491,23 @@ template <class T> struct Sim : SimBase {
                     vs = fmaV(common, mid + Pi, vs);
                     const V3<T> coh = ((-P.mass * P.mass * cohesion_k(P, r)) * rv) * inv_r;
                     const V3<T> curv = (-P.surfaceTension * P.mass) * (ni - nrm[o]);
-                    ts = ts + ((T(2.0f) * P.restDensity) * (coh + curv)) / (ri + ri);
+                    const V3<T> tt = ((T(2.0f) * P.restDensity) * (coh + curv)) / (ri + ri);
+                    ts = ts + tt;
+                    if (track_scales) {
+                        mp += vnorm(common * mid);
+                        mv += vnorm(common * (mid + Pi));
+                        mt += vnorm(tt);
+                    }
                 }
             });
             fp[i] = ps;
             fv[i] = P.viscosity * vs;
             ft[i] = P.surfaceTension * ts;
+            if (track_scales) {
+                sc_fp[i] = T(mp);
+                sc_fv[i] = T(std::fabs(double(P.viscosity)) * mv);
+                sc_ft[i] = T(std::fabs(double(P.surfaceTension)) * mt);
+            }
             fa[i] = mk(T(0), T(0), T(0));
             const T z = -std::fmin(sdf(P, pi), T(0)) * T(0.25f) * P.invParticleSize;
             if (z < T(1)) {
@@ -597,7 +628,8 @@ enum {
 enum {
     ORC_F_POS = 0, ORC_F_VEL, ORC_F_ACC, ORC_F_NORMAL, ORC_F_FPRESSURE, ORC_F_FTENSION, ORC_F_FADHESION,
     ORC_F_FVISCOSITY, ORC_F_COLOUR, ORC_F_VEL_INT,        // vec3 fields
-    ORC_F_DENSITY = 16, ORC_F_PRESSURE, ORC_F_SOUNDSPEED, ORC_F_RHOSUM, // scalar fields
+    ORC_F_DENSITY = 16, ORC_F_PRESSURE, ORC_F_SOUNDSPEED, ORC_F_RHOSUM,  // scalar fields
+    ORC_F_SC_FPRESSURE, ORC_F_SC_FVISCOSITY, ORC_F_SC_FTENSION, ORC_F_SC_NORMAL,  // test scales
     ORC_F_HASH_PRE = 32, ORC_F_HASH, ORC_F_PERM, ORC_F_CELLSTART, ORC_F_CELLOCC, ORC_F_NBRCOUNT  // u32
 };
 
@@ -747,6 +779,10 @@ int orc_get(void* s, int field, float* out_f32, double* out_f64, uint32_t* out_u
             case ORC_F_PRESSURE: sc = &S.prs; break;
             case ORC_F_SOUNDSPEED: sc = &S.cs; break;
             case ORC_F_RHOSUM: sc = &S.rho_sum; break;
+            case ORC_F_SC_FPRESSURE: sc = &S.sc_fp; break;
+            case ORC_F_SC_FVISCOSITY: sc = &S.sc_fv; break;
+            case ORC_F_SC_FTENSION: sc = &S.sc_ft; break;
+            case ORC_F_SC_NORMAL: sc = &S.sc_nrm; break;
             case ORC_F_HASH_PRE: u = &S.hash_pre; break;
             case ORC_F_HASH: u = &S.hash; break;
             case ORC_F_PERM: u = &S.perm; break;
@@ -775,6 +811,8 @@ int orc_get(void* s, int field, float* out_f32, double* out_f64, uint32_t* out_u
     });
     return rc;
 }
+// Test scales of the force and normal sums (Sim::track_scales).
+int orc_track_scales(void* s, int on) { DISPATCH(s, S.track_scales = on != 0); return 0; }
 int orc_set_threads(int n) {
 #ifdef _OPENMP
     if (n > 0) omp_set_num_threads(n);

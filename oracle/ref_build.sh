@@ -4,10 +4,10 @@
 # names of its four __global__ kernels (from the symbol table of a host
 # object of the same translation unit) in oracle/_ref/kernels.txt.
 # Outputs go to oracle/_ref/ only; nothing is copied from the reference tree.
-# Usage: oracle/ref_build.sh [reference root]   (default /root/reference)
+# Usage: oracle/ref_build.sh [reference root]   (default $LIBFLUID_REFERENCE, else /root/reference)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${LIBFLUID_REFERENCE:-/root/reference}}"
 OUT="$HERE/_ref"
 NVCC="${CUDA_HOME:-/usr/local/cuda}/bin/nvcc"
 if [ ! -d "$REF/libfluid/cudasrc" ]; then

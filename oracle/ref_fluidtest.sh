@@ -5,11 +5,11 @@
 # libfluid.so: the drop-in proof.  Also builds oracle/_ref/geo_check, which
 # links the reference's dumpToGeo (main renamed) to compare .geo output.
 # Outputs go to oracle/_ref/ only.
-# Usage: oracle/ref_fluidtest.sh [reference root]   (default /root/reference)
+# Usage: oracle/ref_fluidtest.sh [reference root]   (default $LIBFLUID_REFERENCE, else /root/reference)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 ROOT="$(dirname "$HERE")"
-REF="${1:-/root/reference}"
+REF="${1:-${LIBFLUID_REFERENCE:-/root/reference}}"
 OUT="$HERE/_ref"
 CUDA="${CUDA_HOME:-/usr/local/cuda}"
 CXX="${CXX:-g++}"

@@ -180,7 +180,9 @@ static void alloc(Sim& s) {
 }
 
 // One substep; returns the block size used (0 if nothing was launched).
-static uint32_t substep(const Ref& r, Sim& s, bool count_nbr) {
+// track_perm adds the sort permutation (an index payload) for the parity
+// dumps; timed runs sort exactly fluidsystem.cu:309-313's P, V, A payload.
+static uint32_t substep(const Ref& r, Sim& s, bool count_nbr, bool track_perm) {
     const uint32_t n = s.n;
     CKD(cuMemsetD32((CUdeviceptr)s.occ, 0, s.cells));
     {
@@ -188,12 +190,21 @@ static uint32_t substep(const Ref& r, Sim& s, bool count_nbr) {
         void* args[] = {&op, &s.P, &s.hash, (void*)&n};
         launch(r.hash, dim3((n + 255) / 256), dim3(256), args);
     }
-    thrust::sequence(thrust::device, thrust::device_ptr<uint32_t>(s.idx), thrust::device_ptr<uint32_t>(s.idx) + n);
-    thrust::sort_by_key(thrust::device, thrust::device_ptr<uint32_t>(s.hash), thrust::device_ptr<uint32_t>(s.hash) + n,
-                        thrust::make_zip_iterator(thrust::make_tuple(thrust::device_ptr<float3>(s.P),
-                                                                     thrust::device_ptr<float3>(s.V),
-                                                                     thrust::device_ptr<float3>(s.A),
-                                                                     thrust::device_ptr<uint32_t>(s.idx))));
+    if (track_perm) {
+        thrust::sequence(thrust::device, thrust::device_ptr<uint32_t>(s.idx), thrust::device_ptr<uint32_t>(s.idx) + n);
+        thrust::sort_by_key(thrust::device, thrust::device_ptr<uint32_t>(s.hash),
+                            thrust::device_ptr<uint32_t>(s.hash) + n,
+                            thrust::make_zip_iterator(thrust::make_tuple(thrust::device_ptr<float3>(s.P),
+                                                                         thrust::device_ptr<float3>(s.V),
+                                                                         thrust::device_ptr<float3>(s.A),
+                                                                         thrust::device_ptr<uint32_t>(s.idx))));
+    } else {
+        thrust::sort_by_key(thrust::device, thrust::device_ptr<uint32_t>(s.hash),
+                            thrust::device_ptr<uint32_t>(s.hash) + n,
+                            thrust::make_zip_iterator(thrust::make_tuple(thrust::device_ptr<float3>(s.P),
+                                                                         thrust::device_ptr<float3>(s.V),
+                                                                         thrust::device_ptr<float3>(s.A))));
+    }
     thrust::exclusive_scan(thrust::device, thrust::device_ptr<uint32_t>(s.occ),
                            thrust::device_ptr<uint32_t>(s.occ) + s.cells, thrust::device_ptr<uint32_t>(s.scatter));
     const uint32_t maxOcc = thrust::reduce(thrust::device, thrust::device_ptr<uint32_t>(s.occ),
@@ -291,7 +302,7 @@ int main(int argc, char** argv) {
     if (mode == "run") {
         if (argc < 5) return 1;
         uint32_t bs = 0;
-        for (uint32_t k = 0; k < in.substeps; ++k) bs = substep(r, s, k + 1 == in.substeps);
+        for (uint32_t k = 0; k < in.substeps; ++k) bs = substep(r, s, k + 1 == in.substeps, true);
         char op = 0;
         void* cargs[] = {&op, &s.rho, &s.colour, &s.n};
         launch(r.colour, dim3((s.n + 255) / 256), dim3(256), cargs);
@@ -309,13 +320,13 @@ int main(int argc, char** argv) {
     if (mode == "time") {
         if (argc < 6) return 1;
         const int warm = atoi(argv[4]), steps = atoi(argv[5]);
-        for (int k = 0; k < warm; ++k) substep(r, s, false);
+        for (int k = 0; k < warm; ++k) substep(r, s, false, false);
         CK(cudaDeviceSynchronize());
         cudaEvent_t e0, e1;
         CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
         CK(cudaEventRecord(e0, 0));
         uint32_t bs = 0;
-        for (int k = 0; k < steps; ++k) bs = substep(r, s, false);
+        for (int k = 0; k < steps; ++k) bs = substep(r, s, false, false);
         CK(cudaEventRecord(e1, 0));
         CK(cudaEventSynchronize(e1));
         float ms = 0.f;

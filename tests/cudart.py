@@ -30,6 +30,7 @@ def rt() -> C.CDLL:
         _rt.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
         _rt.cudaMemset.argtypes = [C.c_void_p, C.c_int, C.c_size_t]
         _rt.cudaSetDevice.argtypes = [C.c_int]
+        _rt.cudaMemGetInfo.argtypes = [C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
     return _rt
 
 
@@ -63,3 +64,10 @@ class DeviceBuffer:
 
 def synchronize() -> None:
     _ck(rt().cudaDeviceSynchronize(), "cudaDeviceSynchronize")
+
+
+def mem_get_info() -> tuple[int, int]:
+    """(free, total) bytes of the current device."""
+    free, total = C.c_size_t(), C.c_size_t()
+    _ck(rt().cudaMemGetInfo(C.byref(free), C.byref(total)), "cudaMemGetInfo")
+    return int(free.value), int(total.value)

@@ -9,7 +9,7 @@ from libfluid_gb300 import workloads as W
 
 
 def configure_oracle(o: "oracle.Oracle", spec: W.SceneSpec, pos=None, vel=None):
-    n = spec.n
+    n = spec.n if pos is None else int(np.asarray(pos).reshape(-1, 3).shape[0])
     o.init(n, spec.unit_cube_res or 1)
     if not spec.unit_cube_res:
         o.set_domain(*spec.box, spec.h)
@@ -28,7 +28,7 @@ def configure_oracle(o: "oracle.Oracle", spec: W.SceneSpec, pos=None, vel=None):
 
 
 def configure_gpu(fs, spec: W.SceneSpec, pos=None, vel=None):
-    n = spec.n
+    n = spec.n if pos is None else int(np.asarray(pos).reshape(-1, 3).shape[0])
     fs.init(n, spec.unit_cube_res or 1)
     if not spec.unit_cube_res:
         fs.setDomain(*spec.box, spec.h)
@@ -68,3 +68,83 @@ def scene_invariants(pos, vel, mass, rho=None, rho0=1000.0):
     if rho is not None:
         out["max_rho_dev"] = float(np.max(np.abs(np.asarray(rho, np.float64) / rho0 - 1.0)))
     return out
+
+
+SNAPSHOT_HEADER_BYTES = 128
+
+
+def snapshot_state(fs):
+    """Exact state of a system (sph_snapshot): positions, velocities and
+    accelerations as (n, 3) float32, in the system's slot order."""
+    snap = fs.snapshot()
+    n = fs.numParticles()
+    a = np.frombuffer(snap, np.float32, count=12 * n, offset=SNAPSHOT_HEADER_BYTES).reshape(3, n, 4)
+    return a[0, :, :3].copy(), a[1, :, :3].copy(), a[2, :, :3].copy()
+
+
+def oracle_from_state(precision, spec, pos, vel, acc, scales=True):
+    """An oracle of the scene's parameters holding exactly this state (with
+    the force and normal test scales recorded)."""
+    o = configure_oracle(oracle.Oracle(precision), spec, pos=pos, vel=vel)
+    o.set_state_f64(pos, vel, acc)
+    if scales:
+        o.track_scales(True)
+    return o
+
+
+def by_particle(arr, perm):
+    """A field in sorted order (entry f belongs to the particle that sat in
+    slot perm[f] before the sort) re-indexed by that slot."""
+    out = np.empty_like(arr)
+    out[perm] = arr
+    return out
+
+
+def force_err(g, r, d, sel=None):
+    """(gpu-vs-fp32, gpu-vs-fp64, fp32-vs-fp64) errors of a force field,
+    each relative to max(|F_i|, 1% of the RMS force of the FP32 oracle)."""
+    if sel is not None:
+        g, r, d = g[sel], r[sel], d[sel]
+    scale = float(np.sqrt((r.astype(np.float64) ** 2).sum(1).mean())) if r.size else 0.0
+    floor = max(1e-2 * scale, 1e-30)
+    return rel_err(g, r, floor), rel_err(g, d, floor), rel_err(r, d, floor)
+
+
+# The oracle field holding, per particle, the sum over its pairs of the
+# magnitude of each pair's term (oracle.Oracle.track_scales).
+SCALE_FIELD = {"fpressure": "fpressure_scale", "fviscosity": "fviscosity_scale", "ftension": "ftension_scale",
+               "normal": "normal_scale"}
+
+
+def pair_scale(o32, o64, field):
+    """The pair-term magnitude sum of a field (sorted order), the larger of
+    the FP32 and FP64 oracles' (a pair at r = h that FP32 arithmetic counts
+    and FP64 does not belongs to the FP32 result's scale)."""
+    return np.maximum(o32.get(SCALE_FIELD[field]), o64.get(SCALE_FIELD[field]))
+
+
+def scaled_err(a, b, S):
+    """max_i |a_i - b_i| / S_i, S_i the sum of the magnitudes of particle i's
+    pair terms: a force (or normal) is a sum of about 30 pair terms that
+    largely cancel, so FP32 rounding is proportional to S_i, not to the net
+    |F_i|; a single missing or wrong pair changes F_i by about S_i / 30."""
+    d = np.linalg.norm(np.asarray(a, np.float64) - np.asarray(b, np.float64), axis=1)
+    return float(np.max(d / np.maximum(np.asarray(S, np.float64), 1e-30))) if d.size else 0.0
+
+
+def check_vector_field(label, g, r, d, S, rtol):
+    """A force or normal field, GPU (g) against the FP32 (r) and FP64 (d)
+    oracles.  The bar: within rtol of the FP32 oracle relative to the pair
+    terms' magnitude S (relative to max(|F_i|, 1% RMS) where the field is no
+    pair sum, S None: adhesion), and no further from FP64 than twice the
+    FP32 oracle is.  Both measures are printed."""
+    e_old, e64_old, o64_old = force_err(g, r, d)
+    msg = f"{label}: |F|-relative gpu-vs-fp32 {e_old:.2e}, gpu-vs-fp64 {e64_old:.2e}, fp32-vs-fp64 {o64_old:.2e}"
+    if S is not None:
+        e, e64, o64 = scaled_err(g, r, S), scaled_err(g, d, S), scaled_err(r, d, S)
+        msg += f"; pair-scale-relative gpu-vs-fp32 {e:.2e}, gpu-vs-fp64 {e64:.2e}, fp32-vs-fp64 {o64:.2e}"
+    else:
+        e = e_old
+    print(msg)
+    assert e < rtol, msg
+    assert e64_old <= 2.0 * o64_old + 1e-6, msg

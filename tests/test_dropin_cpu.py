@@ -15,13 +15,15 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = os.path.join("/root/reference", "test", "src", "main.cpp")
+REF_ROOT = os.environ.get("LIBFLUID_REFERENCE", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "test", "src", "main.cpp")
 CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
 @pytest.mark.skipif(not os.path.exists(REF_SRC), reason="reference tree not present")
 def test_reference_fluidtest_compiles_and_geo_matches(tmp_path):
-    r = subprocess.run(["bash", os.path.join(ROOT, "oracle", "ref_fluidtest.sh")], capture_output=True, text=True)
+    r = subprocess.run(["bash", os.path.join(ROOT, "oracle", "ref_fluidtest.sh"), REF_ROOT], capture_output=True,
+                       text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert os.path.exists(os.path.join(ROOT, "oracle", "_ref", "ref_fluidtest"))
     g = subprocess.run([os.path.join(ROOT, "oracle", "_ref", "geo_check"), str(tmp_path)], capture_output=True,
