@@ -533,7 +533,7 @@ def served_requests(count: int, seed: int):
     return specs, [int(x) for x in steps]
 
 
-def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: int = 64) -> dict:
+def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: int = 256) -> dict:
     """Open-loop Poisson arrivals at each rate; p50/p99 latency (arrival to
     final state on the host) and aggregate particle-steps/s, against the
     plain sequential step on the same requests."""
@@ -601,7 +601,10 @@ def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: 
                         "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
                         "throughput": work / (last - first), "offered": rate * work / len(specs),
                         "wall_s": wall, "busy_frac": st["busy_seconds"] / max(last - first, 1e-9),
-                        "peak_live_particles": st["peak_live_particles"]})
+                        "peak_live_particles": st["peak_live_particles"], "iterations": st["iterations"],
+                        "host_seconds": {"admit": st["admit_seconds"], "read": st["read_seconds"],
+                                         "layout": st["layout_seconds"]},
+                        "admit_retries": st["admit_retries"]})
     best = max(r["throughput"] for r in results)
     return {"value": best, "unit": "particle-steps/s",
             "workload": f"{len(specs)} requests: dam breaks as in the batched set, particles log-uniform "

@@ -169,8 +169,10 @@ void Engine::free_all() {
     if (d_params_) cudaFree(d_params_);
     if (d_scenes_) cudaFree(d_scenes_);
     if (d_tiles_) cudaFree(d_tiles_);
-    d_params_ = nullptr; d_scenes_ = nullptr; d_tiles_ = nullptr;
+    if (d_tile_first_) cudaFree(d_tile_first_);
+    d_params_ = nullptr; d_scenes_ = nullptr; d_tiles_ = nullptr; d_tile_first_ = nullptr;
     pcap_ = ccap_ = 0;
+    scene_cap_ = tile_cap_ = tile_first_cap_ = pend_cap_ = 0;
     dev_bytes_ = 0;
 }
 
@@ -407,9 +409,10 @@ int Engine::rebuild_layout() {
     cudaSetDevice(device_);
     const size_t ns = scenes_.size();
     h_scenes_.resize(ns);
-    h_tiles_.clear();
+    h_tile_first_.resize(ns);
     cell_base_.resize(ns);
     uint64_t cb = 0;
+    ntiles_ = 0;
     any_tension_ = false;
     std::vector<uint32_t> h_pend(ns);
     for (size_t k = 0; k < ns; ++k) {
@@ -419,10 +422,10 @@ int Engine::rebuild_layout() {
         cb += s.dp.ncells + 1ull;
         const uint32_t tile = exec_.tile;
         s.table_index = (uint32_t)k;
-        s.tile_first = (uint32_t)h_tiles_.size();
-        for (uint32_t f = 0; f < s.n; f += tile)
-            h_tiles_.push_back(make_uint4((uint32_t)k, s.part_base + f, std::min<uint32_t>(tile, s.n - f), 0u));
-        s.tile_count = (uint32_t)h_tiles_.size() - s.tile_first;
+        s.tile_first = ntiles_;
+        s.tile_count = (s.n + tile - 1u) / tile;
+        h_tile_first_[k] = s.tile_first;
+        ntiles_ += s.tile_count;
         any_tension_ = any_tension_ || (s.dp.flags & 1u);
         h_pend[k] = s.pending ? 1u : 0u;
     }
@@ -443,6 +446,11 @@ int Engine::rebuild_layout() {
         ENG_CK(cudaMallocHost((void**)&h_params_, scene_cap_ * sizeof(DevParams)), "param staging");
         graph_dirty_ = true;
     }
+    if (ns > tile_first_cap_) {
+        if (d_tile_first_) cudaFree(d_tile_first_);
+        tile_first_cap_ = std::max<uint64_t>(ns, tile_first_cap_ * 2);
+        ENG_CK(cudaMalloc((void**)&d_tile_first_, tile_first_cap_ * sizeof(uint32_t)), "tile offsets");
+    }
     if (ns > pend_cap_) {
         if (pend_) cudaFree(pend_);
         pend_cap_ = std::max<uint64_t>(ns, pend_cap_ * 2);
@@ -451,15 +459,19 @@ int Engine::rebuild_layout() {
     }
     if (ns) ENG_CK(cudaMemcpyAsync(pend_, h_pend.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_),
                    "pending flags upload");
-    if (h_tiles_.size() > tile_cap_) {
+    if (ntiles_ > tile_cap_) {
         if (d_tiles_) cudaFree(d_tiles_);
-        tile_cap_ = std::max<uint64_t>(h_tiles_.size(), tile_cap_ * 2);
+        tile_cap_ = std::max<uint64_t>(ntiles_, tile_cap_ * 2);
         ENG_CK(cudaMalloc((void**)&d_tiles_, tile_cap_ * sizeof(uint4)), "tile table");
         graph_dirty_ = true;
     }
     if (ns) ENG_CK(cudaMemcpyAsync(d_scenes_, h_scenes_.data(), ns * sizeof(DevScene), cudaMemcpyHostToDevice, stream_), "scene upload");
-    if (!h_tiles_.empty())
-        ENG_CK(cudaMemcpyAsync(d_tiles_, h_tiles_.data(), h_tiles_.size() * sizeof(uint4), cudaMemcpyHostToDevice, stream_), "tile upload");
+    if (ns) {
+        ENG_CK(cudaMemcpyAsync(d_tile_first_, h_tile_first_.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                               stream_), "tile offsets upload");
+        ENG_CK(launch_build_tiles(d_scenes_, d_tile_first_, (uint32_t)ns, exec_.tile, d_tiles_, stream_),
+               "tile table");
+    }
     ENG_CK(cudaStreamSynchronize(stream_), "layout sync");
     layout_dirty_ = false;
     params_dirty_ = true;
@@ -488,7 +500,7 @@ StepArgs Engine::args() const {
     a.params = d_params_;
     a.scenes = d_scenes_;
     a.tiles = d_tiles_;
-    a.ntiles = (uint32_t)h_tiles_.size();
+    a.ntiles = ntiles_;
     a.total_cells = total_cells_;
     a.P0 = P0_; a.V0 = V0_; a.A0 = A0_;
     a.P1 = P1_; a.V1 = V1_; a.A1 = A1_;

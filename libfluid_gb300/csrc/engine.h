@@ -205,7 +205,10 @@ private:
     DevParams* h_params_ = nullptr;    // pinned
     uint32_t* h_status_ = nullptr;     // pinned
     std::vector<DevScene> h_scenes_;
-    std::vector<uint4> h_tiles_;
+    std::vector<uint32_t> h_tile_first_;   // per scene: its first tile (the tiles are built on the device)
+    uint32_t ntiles_ = 0;
+    uint32_t* d_tile_first_ = nullptr;
+    uint64_t tile_first_cap_ = 0;
     std::vector<uint32_t> cell_base_;
     uint32_t total_cells_ = 0;
     bool any_tension_ = false;

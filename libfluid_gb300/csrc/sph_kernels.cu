@@ -1109,8 +1109,32 @@ __global__ void k_sorted_keys(const DevParams* __restrict__ params, const float4
 }
 
 // ---------------------------------------------------------------------------
+// Tile table of a layout: one block per scene writes that scene's tiles
+// (scene, first slot, count) from its slot range, starting at tile_first[s].
+// The host computes only the per-scene offsets, so a membership change of
+// the served form costs O(scenes) on the host instead of O(tiles).
+// ---------------------------------------------------------------------------
+__global__ void k_build_tiles(const DevScene* __restrict__ scenes, const uint32_t* __restrict__ tile_first,
+                              uint32_t tile, uint4* __restrict__ tiles) {
+    const uint32_t s = blockIdx.x;
+    const DevScene sc = scenes[s];
+    const uint32_t first = tile_first[s];
+    const uint32_t cnt = (sc.n + tile - 1u) / tile;
+    for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+        const uint32_t f = i * tile;
+        tiles[first + i] = make_uint4(s, sc.part_base + f, min(tile, sc.n - f), 0u);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Launch wrappers.
 // ---------------------------------------------------------------------------
+cudaError_t launch_build_tiles(const DevScene* scenes, const uint32_t* tile_first, uint32_t nscenes, uint32_t tile,
+                               uint4* tiles, cudaStream_t st) {
+    if (nscenes == 0) return cudaSuccess;
+    k_build_tiles<<<nscenes, 128, 0, st>>>(scenes, tile_first, tile, tiles);
+    return cudaGetLastError();
+}
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st) {
     k_hash<<<a.ntiles, a.block, 0, st>>>(a.params, a.scenes, a.tiles, a.P0, a.count, a.key, a.slot, a.pend, a.okey,
                                          a.status);

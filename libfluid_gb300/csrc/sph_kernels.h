@@ -50,6 +50,10 @@ struct StepArgs {
 // One-time per-device kernel attributes (call before the first launch).
 cudaError_t init_kernel_attributes();
 
+// The tile table of a layout from the scene table: scene s's tiles start at
+// tile_first[s] (tiles must hold every scene's ceil(n / tile) entries).
+cudaError_t launch_build_tiles(const DevScene* scenes, const uint32_t* tile_first, uint32_t nscenes, uint32_t tile,
+                               uint4* tiles, cudaStream_t st);
 cudaError_t launch_hash(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st);
 // Cells per scan tile, and the most tiles launch_scan_raw takes (k_scan_top

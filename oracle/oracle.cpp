@@ -496,7 +496,11 @@ template <class T> struct Sim : SimBase {
                     if (track_scales) {
                         mp += vnorm(common * mid);
                         mv += vnorm(common * (mid + Pi));
-                        mt += vnorm(tt);
+                        // the curvature term takes the difference of two
+                        // normals, each a cancelling sum with its own scale
+                        mt += std::fabs(double(T(2.0f) * P.restDensity) / double(ri + ri)) *
+                              (vnorm(coh) + std::fabs(double(P.surfaceTension) * double(P.mass)) *
+                                                (double(sc_nrm[i]) + double(sc_nrm[o])));
                     }
                 }
             });

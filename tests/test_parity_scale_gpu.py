@@ -13,7 +13,7 @@ quoted on (the reference step being matched is fluidsystem.cu:301-398):
 * The same 1M particles in the reference's own domain (unit cube, res 100):
   integer fields bit-exact against the reference's own device code
   (oracle/ref_runner driving the unmodified cudasrc kernels), density within
-  1e-5 of it, forces no further from it than twice the FP32 oracle is.
+  1e-5 and forces within 1e-4 of it (relative to the pair terms' magnitude).
 * The ~8M-particle tension scene after three substeps: the GPU state of a
   spatial window (the pool's free surface and the bottom of the first
   sphere) handed to the oracle; hashes and the order of the window's
@@ -26,7 +26,7 @@ import pytest
 
 import oracle
 from helpers import (SCALE_FIELD, by_particle, check_vector_field, configure_gpu, configure_oracle,
-                     oracle_from_state, pair_scale, rel_err, snapshot_state)
+                     oracle_from_state, pair_scale, rel_err, scaled_err, snapshot_state)
 from libfluid_gb300 import FluidSystem, workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -127,7 +127,11 @@ def test_dam_break_1m_unit_cube_against_reference_device_code():
     for f in ("cellstart", "cellocc"):
         assert np.array_equal(fs.debug(f, ncells=nc), ref[f]), f
     o32 = configure_oracle(oracle.Oracle(32), spec)
+    o64 = configure_oracle(oracle.Oracle(64), spec)
+    o32.track_scales(True)
+    o64.track_scales(True)
     o32.advance(spec.dt, 1)
+    o64.advance(spec.dt, 1)
     rho_g = fs.debug("density")
     e = rel_err(rho_g, ref["density"], 1.0)
     print(f"1M unit cube density: gpu-vs-reference {e:.2e}, "
@@ -137,9 +141,16 @@ def test_dam_break_1m_unit_cube_against_reference_device_code():
         g, r, o = fs.debug(f), ref[f], o32.get(f)
         scale = float(np.sqrt((r.astype(np.float64) ** 2).sum(1).mean()))
         floor = max(1e-2 * scale, 1e-30)
-        e_g, e_o = rel_err(g, r, floor), rel_err(o, r, floor)
-        print(f"1M unit cube {f}: gpu-vs-reference {e_g:.2e}, fp32-oracle-vs-reference {e_o:.2e}")
-        assert e_g <= 2.0 * e_o + 1e-5, f
+        msg = (f"1M unit cube {f}: |F|-relative gpu-vs-reference {rel_err(g, r, floor):.2e}, "
+               f"fp32-oracle-vs-reference {rel_err(o, r, floor):.2e}")
+        if f in SCALE_FIELD:
+            S = pair_scale(o32, o64, f)
+            e_g, e_o = scaled_err(g, r, S), scaled_err(o, r, S)
+            msg += f"; pair-scale-relative gpu-vs-reference {e_g:.2e}, fp32-oracle-vs-reference {e_o:.2e}"
+        else:
+            e_g = rel_err(g, r, floor)
+        print(msg)
+        assert e_g < RTOL_FORCE, msg
     pos_g, _, _ = fs.exportToData()
     assert rel_err(pos_g, ref["pos"], 1e-3) < RTOL_POS
     fs.close()
