@@ -762,79 +762,85 @@ k_force_integrate(const DevParams* __restrict__ params,
     const float4 si = S[k];
     const int3 g = grid_of(pp, pi.x, pi.y, pi.z);
     const bool tension = TENSION && (pp.flags & 1u) != 0u;
+    const bool inside = grid_inside(pp, g);
     float fpx = 0.f, fpy = 0.f, fpz = 0.f;   // pressure
     float fvx = 0.f, fvy = 0.f, fvz = 0.f;   // "viscosity" (pressure re-added)
     float ftx = 0.f, fty = 0.f, ftz = 0.f;   // tension
     float fax = 0.f, fay = 0.f, faz = 0.f;   // adhesion
-    if (grid_inside(pp, g)) {
-        const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
-        const float ri = si.x, pri = si.y, csi = si.z;
-        float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (tension) ni = N[k];
-        const float h2 = pp.h2, eps = pp.eps, inv_ri2 = si.w;
-        // 2 rho0 / (rho_i + rho_i) of the tension sum (fluidphysics.cu:293), once per particle
-        const float tden = (2.0f * pp.rest_density) / (ri + ri);
-        const float sm = -pp.surface_tension * pp.mass;
-        const float coh_m = -pp.mass * pp.mass;
-        // per-scene constants of the pair loop, held in registers
-        const float visc = pp.viscosity, hh = pp.h, visc_eps = pp.visc_eps, mass = pp.mass, gsp = pp.grad_spiky;
-        auto run = [&](auto& walk) {
-            uint32_t j;
-            while (walk.next(j)) {
-                // The mask holds exact neighbours, so position, (rho, p, c^2, 1/rho^2)
-                // and velocity of nearly every j are needed: the loads are issued
-                // together, before any test, so their latencies overlap.
-                const float4 pj = __ldg(P1 + j), sj = __ldg(S + j), vj = __ldg(V1 + j);
-                float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (tension) nj = __ldg(N + j);
-                const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
-                const float r2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (r2 <= h2 && r2 > eps && j != k && sj.x > eps) {
-                    // r is the correctly rounded root: h - r below cancels, and pairs at
-                    // r ~ h must see the reference's r; 1/r only scales (approximate)
-                    const float r = sqrtf(r2);
-                    const float inv_r = rsqrtf(r2);
-                    const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
-                    // artificial viscosity -visc (cs_i + cs_j) mu / (rho_i + rho_j),
-                    // mu = h ux / (r^2 + 0.01 h^2), only for approaching pairs;
-                    // evaluated without a branch (finite for every pair) and selected
-                    const float Pv = __fdividef(-visc * (csi + sj.z) * (hh * ux),
-                                                (r2 + visc_eps) * (ri + sj.x));
-                    const float Pi = (ux < 0.0f) ? Pv : 0.0f;
-                    // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
-                    const float mid = sj.y * inv_ri2 + pri * sj.w;
-                    const float gspk = (r >= hh) ? 0.0f : gsp * (hh - r) * (hh - r);   // grad_spiky
-                    const float sr = (mass * gspk) * inv_r;
-                    const float cx = sr * rx, cy = sr * ry, cz = sr * rz;
-                    fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
-                    const float mp = mid + Pi;
-                    fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
-                    if (tension) {
-                        // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
-                        // sigma == 0 the tension force is sigma * (finite sum) = 0, so
-                        // the term is skipped.
-                        const float sc2 = coh_m * cohesion_k(pp, r) * inv_r;
-                        const float hx = sc2 * rx, hy = sc2 * ry, hz = sc2 * rz;
-                        const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
-                        ftx = fmaf(tden, hx + kx, ftx);
-                        fty = fmaf(tden, hy + ky, fty);
-                        ftz = fmaf(tden, hz + kz, ftz);
-                    }
-                }
+    const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
+    const float ri = si.x, pri = si.y, csi = si.z;
+    float4 ni = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tension && inside) ni = N[k];
+    const float h2 = pp.h2, eps = pp.eps, inv_ri2 = si.w;
+    // 2 rho0 / (rho_i + rho_i) of the tension sum (fluidphysics.cu:293), once per particle
+    const float tden = (2.0f * pp.rest_density) / (ri + ri);
+    const float sm = -pp.surface_tension * pp.mass;
+    const float coh_m = -pp.mass * pp.mass;
+    // per-scene constants of the pair loop, held in registers
+    const float visc = pp.viscosity, hh = pp.h, visc_eps = pp.visc_eps, mass = pp.mass, gsp = pp.grad_spiky;
+    // One pair: neighbour j with its position, (rho, p, c^2, 1/rho^2),
+    // velocity and normal.
+    auto pair = [&](uint32_t j, const float4& pj, const float4& sj, const float4& vj, const float4& nj) {
+        const float rx = pj.x - pi.x, ry = pj.y - pi.y, rz = pj.z - pi.z;
+        const float r2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (r2 <= h2 && r2 > eps && j != k && sj.x > eps) {
+            // r is the correctly rounded root: h - r below cancels, and pairs at
+            // r ~ h must see the reference's r; 1/r only scales (approximate)
+            const float r = sqrtf(r2);
+            const float inv_r = rsqrtf(r2);
+            const float ux = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, -rx, -ry, -rz);
+            // artificial viscosity -visc (cs_i + cs_j) mu / (rho_i + rho_j),
+            // mu = h ux / (r^2 + 0.01 h^2), only for approaching pairs;
+            // evaluated without a branch (finite for every pair) and selected
+            const float Pv = __fdividef(-visc * (csi + sj.z) * (hh * ux), (r2 + visc_eps) * (ri + sj.x));
+            const float Pi = (ux < 0.0f) ? Pv : 0.0f;
+            // p_j/rho_i^2 + p_i/rho_j^2 with the reciprocals from the density pass
+            const float mid = sj.y * inv_ri2 + pri * sj.w;
+            const float gspk = (r >= hh) ? 0.0f : gsp * (hh - r) * (hh - r);   // grad_spiky
+            const float sr = (mass * gspk) * inv_r;
+            const float cx = sr * rx, cy = sr * ry, cz = sr * rz;
+            fpx = fmaf(cx, mid, fpx); fpy = fmaf(cy, mid, fpy); fpz = fmaf(cz, mid, fpz);
+            const float mp = mid + Pi;
+            fvx = fmaf(cx, mp, fvx); fvy = fmaf(cy, mp, fvy); fvz = fmaf(cz, mp, fvz);
+            if (tension) {
+                // Akinci cohesion + curvature (fluidphysics.cu:291-293).  With
+                // sigma == 0 the tension force is sigma * (finite sum) = 0, so
+                // the term is skipped.
+                const float sc2 = coh_m * cohesion_k(pp, r) * inv_r;
+                const float hx = sc2 * rx, hy = sc2 * ry, hz = sc2 * rz;
+                const float kx = sm * (ni.x - nj.x), ky = sm * (ni.y - nj.y), kz = sm * (ni.z - nj.z);
+                ftx = fmaf(tden, hx + kx, ftx);
+                fty = fmaf(tden, hy + ky, fty);
+                ftz = fmaf(tden, hz + kz, ftz);
             }
-        };
-        // exact neighbours recorded by the density pass (SPH_MASK_EXACT words)
+        }
+    };
+    // The neighbour's loads are issued together, before any test, so that
+    // their latencies overlap (the masks hold exact neighbours: nearly every
+    // j is used).
+    auto gathered = [&](uint32_t j) {
+        const float4 pj = __ldg(P1 + j), sj = __ldg(S + j), vj = __ldg(V1 + j);
+        float4 nj = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (tension) nj = __ldg(N + j);
+        pair(j, pj, sj, vj, nj);
+    };
+    // exact neighbours recorded by the density pass (SPH_MASK_EXACT words)
+    if (inside) {
         if constexpr (TABLE) {
             extern __shared__ uint32_t s_rows[];
             uint32_t live, full;
             build_row_table(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k,
                             s_rows + threadIdx.x, blockDim.x, live, full);
             TableWalk walk(s_rows + threadIdx.x, blockDim.x, live, full);
-            run(walk);
+            uint32_t j;
+            while (walk.next(j)) gathered(j);
         } else {
             WideMaskWalk walk(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k);
-            run(walk);
+            uint32_t j;
+            while (walk.next(j)) gathered(j);
         }
+    }
+    if (inside) {
         fvx = pp.viscosity * fvx; fvy = pp.viscosity * fvy; fvz = pp.viscosity * fvz;
         ftx = pp.surface_tension * ftx; fty = pp.surface_tension * fty; ftz = pp.surface_tension * ftz;
         const float z = -fminf(sdf(pp, pi.x, pi.y, pi.z), 0.0f) * 0.25f * pp.inv_particle_size;
