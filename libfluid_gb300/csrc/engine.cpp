@@ -507,6 +507,8 @@ StepArgs Engine::args() const {
     a.V2 = V2_; a.S = S_; a.N = N_;
     a.Vc = Vc_; a.okey = okey_; a.pend = pend_;
     a.count = count_; a.start = start_; a.scan_sums = scan_sums_;
+    a.scan_first = 0u;
+    a.scan_cells = 0u;   // all cells
     a.scan_zeroes_counts = 1u;
     a.scan_spin_limit = scan_spin_limit_;
     a.scan_withhold = scan_withhold_ ? 1u : 0u;
@@ -743,6 +745,15 @@ int Engine::prefix_scene(const Scene& sc, bool wait) {
     a.grid_nbr = sc.tile_count;
     a.tile_ctr = nullptr;
     a.scan_zeroes_counts = 0u;   // keep the counts for the full prefix that follows
+    if (hashed_) {
+        // Only this scene's cells hold counts that matter here: scan its own
+        // range (cell starts relative to its first cell, as a full scan
+        // gives them), not the cells of every live scene.  Without a fresh
+        // hash the standalone hash below clears all counts, so the full range
+        // is scanned as before.
+        a.scan_first = cell_base_[sc.table_index];
+        a.scan_cells = sc.dp.ncells + 1u;
+    }
     rc = launch_prefix_args(a, false, !hashed_);
     if (rc) return rc;
     prefix_valid_ = false;

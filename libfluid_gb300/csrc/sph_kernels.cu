@@ -201,14 +201,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* __restri
                                                               unsigned long long* __restrict__ desc,
                                                               uint32_t* __restrict__ out,
                                                               uint32_t* __restrict__ status, uint32_t zero,
-                                                              uint32_t spin_limit) {
+                                                              uint32_t spin_limit, uint32_t vec_ok) {
     __shared__ uint32_t s_tile, s_prefix, s_total;
     __shared__ uint32_t warp_tot[SCAN_THREADS / 32];
     if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int*>(desc), 1u);
     __syncthreads();
     const uint32_t tile = s_tile;
     const uint32_t base = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
-    const bool whole = base + SCAN_ITEMS <= n;   // 16 counts, 64-byte aligned
+    // 16 counts in four 128-bit accesses, when `in` and `out` are 16-byte
+    // aligned (a scene's own range may start anywhere)
+    const bool whole = vec_ok && base + SCAN_ITEMS <= n;
     uint32_t v[SCAN_ITEMS];
     // each count is read (and, with `zero`, cleared at the end) by this thread alone
     if (whole) {
@@ -471,6 +473,20 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         if (rr <= h2) dm |= bit;
         if (SKIN && rr <= skin2) sm |= bit;
     };
+    // Two candidates at once with the packed FP32 instructions of sm_100-class
+    // GPUs (add/mul/fma.rn.f32x2): each component is rounded exactly as the
+    // scalar operation, so r^2 (dot3's fusion order) is the same to the bit.
+    const float2 px2 = make_float2(p.x, p.x), py2 = make_float2(p.y, p.y), pz2 = make_float2(p.z, p.z);
+    auto visit2 = [&](const float4& q0, const float4& q1, uint32_t bit, uint32_t& dm, uint32_t& sm) {
+        const float2 dx = __fadd2_rn(px2, make_float2(-q0.x, -q1.x));
+        const float2 dy = __fadd2_rn(py2, make_float2(-q0.y, -q1.y));
+        const float2 dz = __fadd2_rn(pz2, make_float2(-q0.z, -q1.z));
+        const float2 rr = __ffma2_rn(dz, dz, __ffma2_rn(dx, dx, __fmul2_rn(dy, dy)));
+        if (rr.x <= h2) dm |= bit;
+        if (rr.y <= h2) dm |= bit << 1;
+        if (SKIN && rr.x <= skin2) sm |= bit;
+        if (SKIN && rr.y <= skin2) sm |= bit << 1;
+    };
     // The words of chunk c of row r (bit b = candidate jb0 + 32c + b) minus
     // the particle itself, stored to the masks and the row table.
     auto close_chunk = [&](int r, uint32_t c, uint32_t jb0, uint32_t len, uint32_t dm, uint32_t sm) {
@@ -525,17 +541,14 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                     float4 q0, q1, q2, q3;
                     ld_pos_pair(P1 + jj, q0, q1);
                     ld_pos_pair(P1 + jj + 2u, q2, q3);
-                    visit(q0, bit, dm, sm);
-                    visit(q1, bit << 1, dm, sm);
-                    visit(q2, bit << 2, dm, sm);
-                    visit(q3, bit << 3, dm, sm);
+                    visit2(q0, q1, bit, dm, sm);
+                    visit2(q2, q3, bit << 2, dm, sm);
                     bit <<= 4;
                 }
                 if (jj + 2u <= ce) {
                     float4 q0, q1;
                     ld_pos_pair(P1 + jj, q0, q1);
-                    visit(q0, bit, dm, sm);
-                    visit(q1, bit << 1, dm, sm);
+                    visit2(q0, q1, bit, dm, sm);
                     bit <<= 2;
                     jj += 2u;
                 }
@@ -594,7 +607,10 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     // deferred XSPH of the previous substep (only for particles that had a cell then)
     const uint32_t oi = (__ldg(pend + t.x) != 0u) ? __float_as_uint(vi.w) : SPH_OKEY_NULL;
     const bool xs = oi != SPH_OKEY_NULL;
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    // XSPH sums: x and y packed (f32x2), z alone
+    float2 axy = make_float2(0.f, 0.f);
+    float az = 0.f;
+    const float2 mvixy = make_float2(-vi.x, -vi.y);
     TableWalk walk(tab, ts, live, full);
     uint32_t j;
     while (walk.next(j)) {
@@ -605,7 +621,8 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
         float4 vj = make_float4(0.f, 0.f, 0.f, 0.f);
         if (xs) vj = __ldg(V1 + j);
         const uint32_t oj = __float_as_uint(vj.w);
-        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        const float2 dxy = __fadd2_rn(make_float2(p.x, p.y), make_float2(-q.x, -q.y));
+        const float dx = dxy.x, dy = dxy.y, dz = p.z - q.z;
         const float rr = dot3(dx, dy, dz, dx, dy, dz);
         // true for every recorded bit; the test matters in rows walked in full
         if (rr <= h2 && j != k) {
@@ -618,8 +635,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                 const float rs = p.w + q.w;   // the previous substep's densities
                 if (rs > eps && cells_adjacent_fast(oi, oj)) {
                     const float coeff = w * __fdividef(two_m, rs);
-                    ax = fmaf(coeff, vj.x - vi.x, ax);
-                    ay = fmaf(coeff, vj.y - vi.y, ay);
+                    axy = __ffma2_rn(make_float2(coeff, coeff), __fadd2_rn(make_float2(vj.x, vj.y), mvixy), axy);
                     az = fmaf(coeff, vj.z - vi.z, az);
                 }
             }
@@ -634,7 +650,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     const float cs = pp.gas_constant * powf(ratio, pp.gamma - 1.0f);
     // w = 1/rho^2, used by the force pass for p_j/rho_i^2 + p_i/rho_j^2
     S[k] = make_float4(rho, prs, cs, 1.0f / (rho * rho));
-    Vc[k] = xs ? make_float4(fmaf(pp.xsph, ax, vi.x), fmaf(pp.xsph, ay, vi.y), fmaf(pp.xsph, az, vi.z), 0.f)
+    Vc[k] = xs ? make_float4(fmaf(pp.xsph, axy.x, vi.x), fmaf(pp.xsph, axy.y, vi.y), fmaf(pp.xsph, az, vi.z), 0.f)
                : make_float4(vi.x, vi.y, vi.z, 0.f);
     if (nbr_out) nbr_out[k] = cnt;
   });
@@ -671,7 +687,10 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
         return;
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
+    // x and y packed (f32x2, rounded per component as the scalar operations), z alone
+    float2 sxy = make_float2(0.f, 0.f);
+    float sz = 0.f;
+    const float2 pxy = make_float2(p.x, p.y);
     // m gradPoly6(r) rvec / (rho_j r) = m c (h^2 - r^2)^2 rvec / rho_j: the
     // factor r of gradPoly6 cancels the 1/r; h^2 - r^2 is formed from the
     // rounded root r as gradPoly6 forms it (it cancels near r = h)
@@ -682,14 +701,14 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
         while (walk.next(j)) {
             const float4 q = __ldg(P1 + j);
             const float rhoj = __ldg(&S[j].x);
-            const float rx = p.x - q.x, ry = p.y - q.y, rz = p.z - q.z;
+            const float2 rxy = __fadd2_rn(pxy, make_float2(-q.x, -q.y));
+            const float rx = rxy.x, ry = rxy.y, rz = p.z - q.z;
             const float r2 = dot3(rx, ry, rz, rx, ry, rz);
             if (r2 <= h2 && r2 > eps && j != k && rhoj > eps) {
                 const float r = sqrtf(r2);
                 const float x = fmaf(-r, r, h2);
                 const float s = (r >= h) ? 0.0f : __fdividef(mc * (x * x), rhoj);
-                sx = fmaf(s, rx, sx);
-                sy = fmaf(s, ry, sy);
+                sxy = __ffma2_rn(make_float2(s, s), rxy, sxy);
                 sz = fmaf(s, rz, sz);
             }
         }
@@ -706,7 +725,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
         WideMaskWalk walk(pp, start, sc.cell_base, delta, g, mask + SPH_MASK_EXACT * mask_stride, mask_stride, k);
         run(walk);
     }
-    N[k] = make_float4(pp.h * sx, pp.h * sy, pp.h * sz, 0.f);
+    N[k] = make_float4(pp.h * sxy.x, pp.h * sxy.y, pp.h * sz, 0.f);
   });
 }
 
@@ -1175,8 +1194,11 @@ cudaError_t init_kernel_attributes() {
 // cell is past n), so it reads and writes no count or start, and its
 // descriptor is word nt + 1.
 cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
-    const uint32_t n = a.total_cells;
+    const uint32_t n = a.scan_cells ? a.scan_cells : a.total_cells;
     if (n == 0) return cudaErrorInvalidValue;
+    uint32_t* counts = a.count + a.scan_first;
+    uint32_t* starts = a.start + a.scan_first;
+    const uint32_t vec_ok = ((reinterpret_cast<uintptr_t>(counts) | reinterpret_cast<uintptr_t>(starts)) & 15u) == 0u;
     const uint32_t nt = (n + SCAN_TILE - 1) / SCAN_TILE;
     unsigned long long* desc = reinterpret_cast<unsigned long long*>(a.scan_sums);
     cudaError_t e = cudaMemsetAsync(desc, 0, (size_t)(nt + 2) * sizeof(unsigned long long), st);
@@ -1186,7 +1208,8 @@ cudaError_t launch_scan(const StepArgs& a, cudaStream_t st) {
         if (e != cudaSuccess) return e;
     }
     const uint32_t limit = a.scan_spin_limit ? a.scan_spin_limit : SCAN_SPIN_LIMIT;
-    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(a.count, n, desc, a.start, a.status, a.scan_zeroes_counts, limit);
+    k_scan_single<<<nt, SCAN_THREADS, 0, st>>>(counts, n, desc, starts, a.status, a.scan_zeroes_counts, limit,
+                                                 vec_ok);
     return cudaGetLastError();
 }
 cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_sums, uint32_t* starts,

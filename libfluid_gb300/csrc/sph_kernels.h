@@ -22,6 +22,8 @@ struct StepArgs {
     float4 *S;                 // (rho, p, c^2, 0)
     float4 *N;                 // normals
     uint32_t *count, *start, *scan_sums;
+    uint32_t scan_first;           // the scan covers cells [scan_first, scan_first + scan_cells) (one scene's
+    uint32_t scan_cells;           // range for a single scene's prefix; else 0 and total_cells)
     uint32_t scan_zeroes_counts;   // nonzero: the scan leaves every count it read at zero for the next hash
     uint32_t scan_spin_limit;      // polls of one look-back wait before it gives up (SPH_STATUS_SCAN_TIMEOUT)
     uint32_t scan_withhold;        // test control: tile 0 is never handed out, so waits on it run out
