@@ -616,7 +616,7 @@ def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: 
 
 
 def run_served(args, dist):
-    r = measure_served(dist, args.requests, args.rates, args.manifest)
+    r = measure_served(dist, args.requests, args.rates, args.manifest, plain_sample=args.plain_sample)
     line = {"metric": METRIC, "workload": "served", "unit": "particle-steps/s", "value": r["value"],
             "higher_is_better": True, "n_gpus": dist.world, "dtype": "f32", "data": "synthetic",
             "config": {"workload": r["workload"], "requests": r["requests"], "memory_budget_bytes": 100 << 30,
@@ -655,6 +655,8 @@ def main():
                     help="plain workload: arrival rates (req/s) of its served measurement")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="served workload: number of requests")
+    ap.add_argument("--plain-sample", type=int, default=256,
+                    help="served workload: requests timed alone for the plain sequential rate (evenly spaced)")
     # the knee is near 55 req/s (mean request 1.25e7 particle-steps, ~7e8 particle-steps/s
     # served): two rates below it show unloaded latency, the rest saturation
     ap.add_argument("--rates", type=float, nargs="+", default=[10, 25, 50, 200, 1000],
