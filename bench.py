@@ -311,8 +311,9 @@ def run_ours(args, dist):
     fs = FluidSystem(dist.local)
     configure(fs, spec, pos, vel)
     L = _capi.lib()
-    if args.variant is not None or args.tile is not None:
-        fs.setExec(tile=args.tile or 128, variant=31 if args.variant is None else args.variant)
+    if args.variant is not None or args.tile is not None or args.persistent is not None:
+        fs.setExec(tile=args.tile or 128, persistent=args.persistent or 0,
+                   variant=31 if args.variant is None else args.variant)
 
     # ---- warm-up ----
     for _ in range(args.warmup):
@@ -643,6 +644,8 @@ def main():
                     help="keep the nvidia-smi clock samples of the timed region in this CSV file")
     ap.add_argument("--tile", type=int, default=None, choices=[64, 128, 256],
                     help="plain workload: particles per tile (threads per block; default: the compiled default)")
+    ap.add_argument("--persistent", type=int, default=None,
+                    help="plain workload: persistent blocks per SM of the neighbour passes (default: one block per tile)")
     ap.add_argument("--variant", type=int, default=None,
                     help="plain workload: kernel variant bits (SPH_VARIANT_*; default: the compiled default)")
     ap.add_argument("--skip-systems", action="store_true",
