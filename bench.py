@@ -15,6 +15,8 @@ inputs.  A step is one WCSPH substep of that scene (advance(dt, 1)).
              of positions, colours, velocities to the host).
   cpu_baseline  the CPU oracle (OpenMP restatement of the reference step)
              on a bounded sample of the same scene, on this host's cores.
+  large_tension  the ~8M-particle scene with surface tension (200x200x180
+             pool and two falling spheres), 200 substeps, device-resident.
   batched    256 mixed-size dam breaks (2,048-65,536 particles) advanced by
              one launch per pass for 200 substeps, against the same scenes
              stepped one at a time over the same substeps.
@@ -412,8 +414,10 @@ def run_ours(args, dist):
         refcuda = reference_cuda_compare(args, fs)
 
     # ---- the two systems forms, on their own workloads (rank 0 at N=1) ----
-    batched = served = None
+    batched = served = tension = None
     if not args.skip_systems and dist.world == 1:
+        # the third plain configuration: ~8M particles with surface tension
+        tension = measure_plain(dist, "large_tension", args.batched_steps, 5)
         batched = measure_batched(dist, args.scenes, args.batched_steps, 3)
         served = measure_served(dist, args.served_requests, args.served_rates)
 
@@ -432,7 +436,7 @@ def run_ours(args, dist):
                        "parallelism": "replicas" if dist.world > 1 else "single GPU",
                        "timing": "CUDA events on the library stream, graph replay"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "reference_cuda": refcuda,
-            "batched": batched, "served": served,
+            "large_tension": tension, "batched": batched, "served": served,
             "gpu_launches": launches_per_substep * args.steps, "clocks": clk,
             "passes_ms_per_substep": per_launch,
             "published_reference": {"value": 7.7e7, "unit": "particle-steps/s",
@@ -440,6 +444,28 @@ def run_ours(args, dist):
                                             "unstated, so not the same configuration"}}
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def measure_plain(dist, workload_name: str, steps: int, warmup: int) -> dict:
+    """Another plain scene of the same library (device-resident state, graph
+    replay, CUDA events on the library's stream)."""
+    from libfluid_gb300 import FluidSystem
+    spec, desc = workload(workload_name)
+    fs = FluidSystem(dist.local)
+    configure(fs, spec, spec.positions(), spec.velocities())
+    for _ in range(warmup):
+        fs.advance(spec.dt, 1)
+    fs.sync()
+    fs.timerMark(0)
+    for _ in range(steps):
+        fs.advanceAsync(spec.dt, 1)
+    fs.timerMark(1)
+    ms = fs.timerElapsed(0, 1)
+    fs.sync()
+    fs.close()
+    return {"workload": desc, "particles": spec.n, "value": spec.n * steps / (ms * 1e-3), "unit": "particle-steps/s",
+            "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+            "timing": "CUDA events on the library stream, graph replay"}
 
 
 BATCH_DESC = ("dam-break scenes, particles log-uniform [2048, 65536], aspect [0.5,2], box 2x/1.2x the block, "
@@ -534,7 +560,7 @@ def served_requests(count: int, seed: int):
     return specs, [int(x) for x in steps]
 
 
-def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: int = 256) -> dict:
+def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: int = 1 << 30) -> dict:
     """Open-loop Poisson arrivals at each rate; p50/p99 latency (arrival to
     final state on the host) and aggregate particle-steps/s, against the
     plain sequential step on the same requests."""
@@ -544,14 +570,16 @@ def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: 
     from libfluid_gb300.server import Server
     specs, steps = served_requests(num_requests, seed=13)
     work = sum(s.n * k for s, k in zip(specs, steps))
-    # plain sequential step: per-substep device time of each sampled request
-    # alone (graph replay), times its substeps
+    # plain sequential step: per-substep device time of each request alone
+    # (graph replay), times its substeps; every request by default (a sample
+    # of a few hundred moved the rate by 10-15%: it follows the mean scene
+    # size).  One engine serves them in turn, each scene alone in it.
     plain_ms = 0.0
-    sample = list(range(0, len(specs), max(1, len(specs) // plain_sample)))
+    sample = list(range(0, len(specs), max(1, len(specs) // max(1, plain_sample))))
     sample_work = 0
+    one = Batch(dist.local)
     for i in sample:
-        one = Batch(dist.local)
-        one.add_scene(specs[i])
+        sid = one.add_scene(specs[i])
         for _ in range(3):
             one.step(1)
         one.sync()
@@ -561,7 +589,8 @@ def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: 
         one.timer_mark(1)
         plain_ms += one.timer_elapsed(0, 1) / 20 * steps[i]
         sample_work += specs[i].n * steps[i]
-        one.close()
+        one.remove_scene(sid)
+    one.close()
     plain_rate = sample_work / (plain_ms * 1e-3)
     results = []
     rng = np.random.default_rng(99)
@@ -611,8 +640,10 @@ def measure_served(dist, num_requests: int, rates, manifest=None, plain_sample: 
             "workload": f"{len(specs)} requests: dam breaks as in the batched set, particles log-uniform "
                         "[1024, 262144], substeps U[50,500], open-loop Poisson arrivals, 100 GB budget",
             "requests": len(specs), "offered_particle_steps": work,
-            "plain_sequential": {"value": plain_rate, "how": f"{len(sample)} requests alone, per-substep device "
-                                                             "time x their substeps"},
+            "plain_sequential": {"value": plain_rate, "requests": len(sample),
+                                 "how": f"{len(sample)} of the {len(specs)} requests alone in one engine, per-substep "
+                                        "device time of 20 substeps after 3 of warm-up (graph replay) x their "
+                                        "substeps"},
             "speedup_vs_plain": best / plain_rate, "rates": results}
 
 
@@ -658,8 +689,9 @@ def main():
                     help="plain workload: arrival rates (req/s) of its served measurement")
     ap.add_argument("--scenes", type=int, default=256, help="batched workload: number of scenes")
     ap.add_argument("--requests", type=int, default=400, help="served workload: number of requests")
-    ap.add_argument("--plain-sample", type=int, default=256,
-                    help="served workload: requests timed alone for the plain sequential rate (evenly spaced)")
+    ap.add_argument("--plain-sample", type=int, default=1 << 30,
+                    help="served workload: requests timed alone for the plain sequential rate (evenly spaced; "
+                         "default: all of them)")
     # the knee is near 55 req/s (mean request 1.25e7 particle-steps, ~7e8 particle-steps/s
     # served): two rates below it show unloaded latency, the rest saturation
     ap.add_argument("--rates", type=float, nargs="+", default=[10, 25, 50, 200, 1000],
