@@ -68,3 +68,37 @@ def test_dam_break_multistep(unit_cube, steps):
         assert abs(g["max_rho_dev"] - d["max_rho_dev"]) <= max(FACTOR * rho_ref, RHO_FLOOR)
     finally:
         fs.close()
+
+
+def test_dam_break_1m_multistep():
+    """The 1,000,000-particle dam break of the benchmark (2x1x1 m box,
+    substeps of 1e-4 s) for 100 substeps on the benchmarked path (deferred
+    XSPH, CUDA graphs), against both oracles on the same bounds."""
+    spec = W.dam_break_1m(seed=23)
+    steps = 100
+    fs = FluidSystem(0)
+    configure_gpu(fs, spec)
+    o32 = configure_oracle(oracle.Oracle(32), spec)
+    o64 = configure_oracle(oracle.Oracle(64), spec)
+    try:
+        for _ in range(steps):
+            assert fs.advance(spec.dt, 1) == 1
+            o32.advance(spec.dt, 1)
+            o64.advance(spec.dt, 1)
+        pos, _, vel = fs.exportToData()
+        g = scene_invariants(pos, vel, spec.mass, rho=gpu_density(fs, spec.n), rho0=spec.rest_density)
+        a = _invariants_oracle(o32, spec)
+        d = _invariants_oracle(o64, spec)
+        print(f"1M dam break, {steps} substeps")
+        for key in ("mass", "kinetic", "max_rho_dev"):
+            print(f"  {key}: gpu {g[key]:.6e}  fp32 {a[key]:.6e}  fp64 {d[key]:.6e}")
+        print(f"  com: gpu {g['com']}  fp32 {a['com']}  fp64 {d['com']}")
+        assert g["mass"] == pytest.approx(d["mass"], rel=1e-12)
+        kin_ref = abs(a["kinetic"] - d["kinetic"])
+        assert abs(g["kinetic"] - d["kinetic"]) <= max(FACTOR * kin_ref, KIN_FLOOR * d["kinetic"])
+        com_ref = float(np.max(np.abs(a["com"] - d["com"])))
+        assert float(np.max(np.abs(g["com"] - d["com"]))) <= max(FACTOR * com_ref, COM_FLOOR)
+        rho_ref = abs(a["max_rho_dev"] - d["max_rho_dev"])
+        assert abs(g["max_rho_dev"] - d["max_rho_dev"]) <= max(FACTOR * rho_ref, RHO_FLOOR)
+    finally:
+        fs.close()
