@@ -531,8 +531,9 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                 const uint32_t ce = min(cb + 32u, je0);
                 uint32_t dm = 0u, sm = 0u, bit = 1u;
                 uint32_t jj = cb;
-                // from an even slot on, two candidates per 256-bit load
-                if ((jj & 1u) != 0u) {
+                // from an even slot on, two candidates per 256-bit load (an
+                // empty row runs this body once, with cb == ce: no candidate)
+                if (jj < ce && (jj & 1u) != 0u) {
                     visit(__ldg(P1 + jj), bit, dm, sm);
                     bit <<= 1;
                     ++jj;
