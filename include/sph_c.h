@@ -35,7 +35,7 @@ enum sph_status {
     SPH_ENAN = 4,      /* a non-finite particle position appeared */
     SPH_ETIMEOUT = 5,  /* a bounded wait ran out */
     SPH_ENOTINIT = 6,  /* advance/export before init (the reference silently returns) */
-    SPH_ECELL = 7,     /* a grid cell held more particles than supported (8192) */
+    SPH_ECELL = 7,     /* a grid cell held more than 8192 particles; the substep left them as they were */
     SPH_EBUSY = 8      /* request rejected: over capacity */
 };
 
@@ -84,7 +84,9 @@ int64_t sph_substep_count(float full_dt, uint32_t substeps);
 /* ---- readback ---------------------------------------------------------- */
 /* FluidSystem::exportToData (fluidsystem.cu:154-173): positions, density
  * colour (DensityColourOperator, fluidutil.cu:67-80) and velocities in the
- * order of the last substep's cell sort.  Any pointer may be NULL. */
+ * order of the last substep's cell sort.  Any pointer may be NULL.  Returns
+ * once the buffers are filled; the next substep's force pass may then be
+ * running already (sph_set_export_ahead). */
 int sph_export(sph_system* s, float* pos, float* colour, float* vel, uint32_t n);
 /* Houdini PGEOMETRY V5 export of one frame, byte-identical to fluidtest's
  * dumpToGeo (test/src/main.cpp:10-74): pos/colour/vel packed xyz, n points.
@@ -198,7 +200,8 @@ enum sph_field {
  * fields (hash, perm, cell start and occupancy) and density, pressure and
  * sound speed describe the most recent sort, which after a blocking advance
  * or an export is already the next substep's (its prefix runs early, see
- * sph_advance). */
+ * sph_advance), and after an export the normals may be the next substep's
+ * too (sph_set_export_ahead). */
 int sph_debug_enable(sph_system* s, int on);
 int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count);
 /* Test control of the error path of the cell scan (no counterpart: the
@@ -244,6 +247,14 @@ int sph_set_exec(sph_system* s, const sph_exec_config* e);
 int sph_set_deferred_xsph(sph_system* s, int on);
 int sph_get_exec(const sph_system* s, sph_exec_config* e);
 int sph_set_use_graph(sph_system* s, int on);     /* CUDA-graph replay of the substep (default on) */
+/* Export ahead (no counterpart; on != 0 is the default).  An export of
+ * velocities after a blocking advance waits for the next substep's density
+ * pass, which computes the XSPH update.  With this on, that export also
+ * starts the next substep's normal and force passes while the velocities
+ * cross the host link.  The next advance takes them as its first substep
+ * when no parameter changed; every other call first undoes them exactly.
+ * Results are the same bit for bit either way. */
+int sph_set_export_ahead(sph_system* s, int on);
 int sph_set_profiling(sph_system* s, int on);     /* per-pass CUDA events (disables the graph) */
 /* Accumulated per-pass milliseconds since profiling was enabled, in the
  * order hash, scan, sort, density, normals, force_integrate, xsph, substep. */

@@ -217,6 +217,11 @@ class FluidSystem:
     def setUseGraph(self, on: bool) -> None:
         self._ck(self._L.sph_set_use_graph(self._h, 1 if on else 0))
 
+    def setExportAhead(self, on: bool) -> None:
+        """Let an export of velocities start the next substep's force pass
+        (default on; results are identical either way)."""
+        self._ck(self._L.sph_set_export_ahead(self._h, 1 if on else 0))
+
     def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 31) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)

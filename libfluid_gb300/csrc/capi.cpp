@@ -417,13 +417,15 @@ int sph_debug_get(sph_system* s, int field, void* buf, uint64_t count) {
 }
 int sph_debug_scan_fault(sph_system* s, uint32_t spin_limit, int withhold_first_tile) {
     if (!s) return SPH_EINVAL;
-    s->eng->set_scan_fault(spin_limit, withhold_first_tile != 0);
-    return SPH_OK;
+    return eng_err(s, s->eng->set_scan_fault(spin_limit, withhold_first_tile != 0));
 }
 int sph_set_use_graph(sph_system* s, int on) {
     if (!s) return SPH_EINVAL;
-    s->eng->set_use_graph(on != 0);
-    return SPH_OK;
+    return eng_err(s, s->eng->set_use_graph(on != 0));
+}
+int sph_set_export_ahead(sph_system* s, int on) {
+    if (!s) return SPH_EINVAL;
+    return eng_err(s, s->eng->set_export_ahead(on != 0));
 }
 int sph_set_deferred_xsph(sph_system* s, int on) {
     if (!s) return SPH_EINVAL;

@@ -184,8 +184,7 @@ int sph_batch_debug_get(sph_batch* b, int scene_id, int field, void* buf, uint64
 }
 int sph_batch_set_use_graph(sph_batch* b, int on) {
     if (!b) return SPH_EINVAL;
-    b->eng->set_use_graph(on != 0);
-    return SPH_OK;
+    return berr(b, b->eng->set_use_graph(on != 0));
 }
 int sph_batch_set_deferred_xsph(sph_batch* b, int on) {
     if (!b) return SPH_EINVAL;

@@ -113,9 +113,12 @@ Engine::Engine(int device) {
     cudaStreamCreateWithFlags(&copy_stream_, cudaStreamNonBlocking);
     cudaEventCreateWithFlags(&copy_ev_, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&suffix_ev_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&pack_ev_, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&vel_ev_, cudaEventDisableTiming);
     cudaMallocHost((void**)&h_status_, sizeof(uint32_t));
-    cudaMalloc((void**)&status_, sizeof(uint32_t));
-    cudaMemsetAsync(status_, 0, sizeof(uint32_t), stream_);
+    cudaMalloc((void**)&status_, 2 * sizeof(uint32_t));
+    cudaMemsetAsync(status_, 0, 2 * sizeof(uint32_t), stream_);
+    gate_ = status_ + 1;
     cudaMalloc((void**)&scal_, 8 * sizeof(uint32_t));
     cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_);
     for (auto& e : ev_) cudaEventCreate(&e);
@@ -139,6 +142,8 @@ Engine::~Engine() {
     if (h_params_) cudaFreeHost(h_params_);
     if (copy_ev_) cudaEventDestroy(copy_ev_);
     if (suffix_ev_) cudaEventDestroy(suffix_ev_);
+    if (pack_ev_) cudaEventDestroy(pack_ev_);
+    if (vel_ev_) cudaEventDestroy(vel_ev_);
     if (copy_stream_) cudaStreamDestroy(copy_stream_);
     if (stream_) cudaStreamDestroy(stream_);
 }
@@ -327,6 +332,7 @@ int Engine::set_exec(const ExecConfig& e) {
     if (!(e.skin > 0.0f && e.skin <= 1.0f)) return fail(ENG_EINVAL, "skin must be in (0, 1]");
     if (e.persistent > 64) return fail(ENG_EINVAL, "persistent blocks per SM must be <= 64");
     if (e.variant & ~SPH_VARIANT_MASK) return fail(ENG_EINVAL, "unknown kernel variant bits");
+    if (const int rc = settle()) return rc;
     if (e.tile != exec_.tile) layout_dirty_ = true;
     graph_dirty_ = true;
     exec_ = e;
@@ -339,6 +345,7 @@ int Engine::set_exec(const ExecConfig& e) {
 }
 
 int Engine::add_scene(const SceneConfig& cfg_in, uint32_t n, int* id_out) {
+    if (const int rc = settle()) return rc;
     Scene s;
     std::string e;
     SceneConfig cfg = cfg_in;
@@ -362,6 +369,7 @@ int Engine::add_scene(const SceneConfig& cfg_in, uint32_t n, int* id_out) {
 }
 
 int Engine::remove_scene(int id) {
+    if (const int rc = settle()) return rc;
     for (size_t k = 0; k < scenes_.size(); ++k) {
         if (scenes_[k].id == id) {
             free_slots(scenes_[k].part_base, scenes_[k].n);
@@ -388,6 +396,7 @@ int Engine::set_config(int id, const SceneConfig& cfg_in) {
         }
         // a pending XSPH update belongs to the substep that ran with the old
         // parameters: apply it before they change
+        if (const int rc = settle()) return rc;
         if (s.pending) { int rc = materialize(s); if (rc) return rc; }
         prefix_valid_ = false;
         if (dp.ncells != s.dp.ncells || dp.flags != s.dp.flags) layout_dirty_ = true;
@@ -561,8 +570,9 @@ int Engine::launch_prefix_args(const StepArgs& a, bool profile, bool hash) {
     return ENG_OK;
 }
 
-int Engine::launch_suffix(bool profile) {
-    const StepArgs a = args();
+int Engine::launch_suffix(bool profile) { return launch_suffix_args(args(), profile); }
+
+int Engine::launch_suffix_args(const StepArgs& a, bool profile) {
     cudaStream_t st = stream_;
     auto mark = [&](int i) { if (profile) cudaEventRecord(ev_[i], st); };
     if (any_tension_) ENG_CK(launch_normals(a, st), "normals");
@@ -588,6 +598,24 @@ int Engine::read_status() {
         if (st & SPH_STATUS_NONFINITE) return fail(ENG_ENAN, "non-finite particle position");
         if (st & SPH_STATUS_SCAN_TIMEOUT) return fail(ENG_ETIMEOUT, "cell scan: a look-back wait ran out");
     }
+    return ENG_OK;
+}
+
+// The passes an export ran ahead (get_state) are undone: the state goes back
+// to the prefix's gathered copies, and the cell counts, tile counters and
+// hash that the force pass produced are cleared; the prefix itself stays
+// valid.  Its status word (gate_) is dropped with it.
+int Engine::settle() {
+    if (!ahead_) return ENG_OK;
+    ahead_ = false;
+    cudaSetDevice(device_);
+    const Scene& s = scenes_.front();
+    ENG_CK(launch_undo_ahead(args(), s.tile_first, s.tile_count, stream_), "undo");
+    ENG_CK(cudaMemsetAsync(count_, 0, (size_t)total_cells_ * sizeof(uint32_t), stream_), "memset counts");
+    ENG_CK(cudaMemsetAsync(scal_, 0, 8 * sizeof(uint32_t), stream_), "memset substep scalars");
+    hashed_ = false;
+    // an export that follows waits for this event before it packs the state
+    ENG_CK(cudaEventRecord(suffix_ev_, stream_), "undo event");
     return ENG_OK;
 }
 
@@ -640,13 +668,29 @@ int Engine::prepare_work() {
 int Engine::step(uint32_t substeps, bool sync) {
     cudaSetDevice(device_);
     if (scenes_.empty()) return ENG_OK;
+    // The passes an export ran ahead are this step's first substep when the
+    // layout and parameters are those they ran with; their status word joins
+    // this step's (the export found it clear).
+    bool taken = false;
+    if (ahead_) {
+        if (substeps > 0 && !layout_dirty_ && !params_dirty_ && prefix_valid_) {
+            ahead_ = false;
+            taken = true;
+            ENG_CK(cudaMemcpyAsync(status_, gate_, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream_),
+                   "status merge");
+        } else if (const int rc = settle()) {
+            return rc;
+        }
+    }
     if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
     int rc = prepare();
     if (rc) return rc;
     const bool graph = use_graph_ && !profiling_;
     eager_prefix_ = false;
     for (uint32_t s = 0; s < substeps; ++s) {
-        if (graph) {
+        if (s == 0 && taken) {
+            // normals and forces ran ahead; nothing to launch
+        } else if (graph) {
             if (!prefix_valid_) {
                 if (!hashed_) { rc = launch_hash_standalone(args()); if (rc) return rc; }
                 ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
@@ -768,7 +812,8 @@ int Engine::materialize(Scene& s) {
     int rc = ensure_prefix();
     if (rc) return rc;
     const StepArgs a = args();
-    ENG_CK(launch_unsort_vel(a, s.tile_first, s.tile_count, s.part_base, nullptr, V0_, true, stream_), "materialize");
+    ENG_CK(launch_unsort_vel(a, s.tile_first, s.tile_count, s.part_base, s.n, nullptr, V0_, true, stream_),
+           "materialize");
     ENG_CK(cudaStreamSynchronize(stream_), "materialize sync");
     s.pending = false;
     return ENG_OK;
@@ -784,6 +829,7 @@ int Engine::materialize_all() {
 
 int Engine::set_deferred_xsph(bool on) {
     if (on == defer_xsph_) return ENG_OK;
+    if (const int rc = settle()) return rc;
     if (!on) { int rc = materialize_all(); if (rc) return rc; }
     defer_xsph_ = on;
     params_dirty_ = true;
@@ -797,6 +843,7 @@ int Engine::sync() {
 }
 
 int Engine::set_profiling(bool on) {
+    if (const int rc = settle()) return rc;
     profiling_ = on;
     for (double& v : pass_ms_) v = 0.0;
     prof_substeps_ = 0;
@@ -839,6 +886,7 @@ Scene* Engine::mscene(int id) {
 
 int Engine::set_state(int id, const float* pos, const float* vel, uint32_t n, bool from_device) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
@@ -865,6 +913,7 @@ int Engine::set_state(int id, const float* pos, const float* vel, uint32_t n, bo
 
 int Engine::set_positions(int id, uint32_t first, const float* pos, uint32_t count) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if ((uint64_t)first + count > s->n) return fail(ENG_EINVAL, "range exceeds the scene's particle count");
@@ -885,6 +934,7 @@ int Engine::set_positions(int id, uint32_t first, const float* pos, uint32_t cou
 
 int Engine::generate_lattice(int id, const LatticeSpec& spec, uint32_t first) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     const uint64_t n = (uint64_t)spec.nx * spec.ny * spec.nz;
@@ -898,6 +948,7 @@ int Engine::generate_lattice(int id, const LatticeSpec& spec, uint32_t first) {
 
 int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n, bool to_device) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
@@ -918,7 +969,7 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
         const StepArgs a = args();
         ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, pos, colour, pend ? nullptr : vel,
                            stream_), "pack");
-        if (pend) ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, vel, nullptr, false,
+        if (pend) ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, s->n, vel, nullptr, false,
                                            stream_), "unsort");
         ENG_CK(cudaStreamSynchronize(stream_), "pack sync");
         return ENG_OK;
@@ -938,20 +989,49 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
         // suffix_ev_: the state it ended with (P0; V0 when no update is
         // pending) is packed and copied on the copy stream meanwhile, and a
         // pending update's velocities follow the prefix on the main stream.
+        // Export ahead (set_export_ahead): the velocities cross the host link
+        // on the copy stream while the main stream runs the next substep's
+        // normal and force passes, with their own status word, which starts
+        // failed when the prefix reported an error; they write the state
+        // only after the pack has read it.
+        const bool ahead = pend && ahead_enabled_ && all_defer_ && use_graph_ && !profiling_ && !debug_ &&
+                           scenes_.size() == 1;
         ENG_CK(cudaStreamWaitEvent(copy_stream_, suffix_ev_, 0), "export wait");
         ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, pend ? nullptr : dv,
                            copy_stream_), "pack");
+        if (ahead) ENG_CK(cudaEventRecord(pack_ev_, copy_stream_), "pack event");
         if (pos) ENG_CK(cudaMemcpyAsync(pos, dp, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
         if (colour) ENG_CK(cudaMemcpyAsync(colour, dc, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
         if (vel && !pend) ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
         if (pend) {
             const StepArgs a = args();
-            ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, dv, nullptr, false, stream_),
+            ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, s->n, dv, nullptr, false, stream_,
+                                     ahead ? gate_ : nullptr),
                    "unsort");
-            ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+            if (ahead) {
+                ENG_CK(cudaEventRecord(vel_ev_, stream_), "unsort event");
+                ENG_CK(cudaStreamWaitEvent(copy_stream_, vel_ev_, 0), "export wait");
+                ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, copy_stream_), "download");
+                ENG_CK(cudaMemcpyAsync(h_status_, status_, sizeof(uint32_t), cudaMemcpyDeviceToHost, copy_stream_),
+                       "status read");
+                ENG_CK(cudaStreamWaitEvent(stream_, pack_ev_, 0), "ahead wait");
+                StepArgs b = a;
+                b.status = gate_;
+                rc = launch_suffix_args(b, false);
+                if (rc) return rc;
+                ahead_ = true;
+            } else {
+                ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
+            }
         }
         const cudaError_t ce = cudaStreamSynchronize(copy_stream_);
         if (ce != cudaSuccess) return cuda_fail(ce, "download sync");
+        if (ahead_) {
+            if (*h_status_ == 0u) return ENG_OK;
+            // the passes run ahead found their status word failed and did
+            // nothing: report the prefix's error as below
+            ahead_ = false;
+        }
         rc = read_status();   // the prefix's status; waits for the main stream too
         if (rc) { prefix_valid_ = false; eager_prefix_ = false; return rc; }
         return ENG_OK;
@@ -975,7 +1055,7 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
     rc = run_prefix(false);
     if (rc == ENG_OK) {
         const StepArgs a = args();
-        ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, dv, nullptr, false, stream_),
+        ENG_CK(launch_unsort_vel(a, s->tile_first, s->tile_count, s->part_base, s->n, dv, nullptr, false, stream_),
                "unsort");
         ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
     }
@@ -989,6 +1069,7 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
 
 int Engine::save_state(int id, float4* host, uint32_t n) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
@@ -1007,6 +1088,7 @@ int Engine::save_state(int id, float4* host, uint32_t n) {
 
 int Engine::load_state(int id, const float4* host, uint32_t n) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     Scene* s = mscene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");
     if (n != s->n) return fail(ENG_EINVAL, "particle count mismatch");
@@ -1024,6 +1106,7 @@ int Engine::load_state(int id, const float4* host, uint32_t n) {
 
 int Engine::debug_enable(bool on) {
     if (on == debug_) return ENG_OK;
+    if (const int rc = settle()) return rc;
     // debug taps show each substep's own passes: XSPH runs in every substep
     if (on) { int rc = materialize_all(); if (rc) return rc; }
     debug_ = on;
@@ -1039,6 +1122,7 @@ int Engine::debug_enable(bool on) {
 
 int Engine::debug_get(int id, int field, void* host, uint64_t count) {
     cudaSetDevice(device_);
+    if (const int rc = settle()) return rc;
     ENG_CK(cudaStreamSynchronize(stream_), "debug sync");
     const Scene* s = scene(id);
     if (!s) return fail(ENG_EINVAL, "unknown scene id");

@@ -103,15 +103,35 @@ public:
     // wait (0: the default), and with `withhold` no block takes the first
     // tile, so every wait that reaches it runs out and the step reports
     // ENG_ETIMEOUT with the state as it was before the failed substep.
-    void set_scan_fault(uint32_t spin_limit, bool withhold) {
+    int set_scan_fault(uint32_t spin_limit, bool withhold) {
+        const int rc = settle();
         scan_spin_limit_ = spin_limit;
         scan_withhold_ = withhold;
         graph_dirty_ = true;
         prefix_valid_ = false;
+        return rc;
     }
 
     // Options.
-    void set_use_graph(bool on) { use_graph_ = on; graph_dirty_ = true; }
+    int set_use_graph(bool on) {
+        const int rc = settle();
+        use_graph_ = on;
+        graph_dirty_ = true;
+        return rc;
+    }
+    // Export ahead (on by default).  A blocking export of a single scene
+    // whose velocities wait for the XSPH update (deferred XSPH) starts the
+    // next substep's normal and force passes once that update is computed,
+    // so that they run while the velocities cross the host link.  The next
+    // step() takes them as its first substep when nothing changed in
+    // between; every other call first undoes them exactly (settle()), so
+    // results do not depend on this option.
+    int set_export_ahead(bool on) {
+        const int rc = settle();
+        ahead_enabled_ = on;
+        return rc;
+    }
+    bool export_ahead() const { return ahead_enabled_; }
     int set_exec(const ExecConfig& e);
     const ExecConfig& exec() const { return exec_; }
     int sm_count() const { return sm_count_; }
@@ -137,7 +157,10 @@ public:
     // Cap on the arena footprint (0 = none): growth beyond it fails with ENG_ENOMEM.
     void set_byte_limit(uint64_t bytes) { byte_limit_ = bytes; }
     // Grow the arenas to at least this many particle slots and cells now.
-    int reserve(uint64_t parts, uint64_t cells) { return ensure_capacity(parts, cells); }
+    int reserve(uint64_t parts, uint64_t cells) {
+        if (const int rc = settle()) return rc;
+        return ensure_capacity(parts, cells);
+    }
 
 private:
     int fail(int code, const std::string& msg);
@@ -150,6 +173,10 @@ private:
     int launch_hash_standalone(const StepArgs& a);
     int prefix_scene(const Scene& s, bool wait = true);  // the prefix over one scene's tiles
     int launch_suffix(bool profile);   // normals, force + integrator, [XSPH]
+    int launch_suffix_args(const StepArgs& a, bool profile);
+    // Undo the passes an export ran ahead, if any (see set_export_ahead):
+    // every entry point but step() and sync() calls this first.
+    int settle();
     int ensure_prefix(bool wait = true);   // the next substep's prefix, computed once
     int materialize(Scene& s);         // apply a pending XSPH update to the state
     int materialize_all();
@@ -174,6 +201,8 @@ private:
     cudaStream_t copy_stream_ = nullptr;   // exports: copies that overlap the prefix
     cudaEvent_t copy_ev_ = nullptr;
     cudaEvent_t suffix_ev_ = nullptr;      // the last blocking step's suffix (and status read) done
+    cudaEvent_t pack_ev_ = nullptr;        // an export's pack of the state done (export ahead)
+    cudaEvent_t vel_ev_ = nullptr;         // an export's velocities unsorted (export ahead)
     std::string err_;
     std::vector<Scene> scenes_;
     int next_id_ = 1;
@@ -187,6 +216,7 @@ private:
     uint32_t *pend_ = nullptr;                      // per scene-table entry: XSPH update pending
     uint32_t *key_ = nullptr, *slot_ = nullptr, *tmp_ = nullptr, *perm_ = nullptr;
     uint32_t *count_ = nullptr, *start_ = nullptr, *scan_sums_ = nullptr, *status_ = nullptr;
+    uint32_t *gate_ = nullptr;        // status word of the passes an export ran ahead (status_ + 1)
     uint32_t *mask_ = nullptr;        // SPH_MASK_ROWS neighbour-mask words per slot
     uint32_t *scal_ = nullptr;        // per-substep scalars: [0] displacement max, [4..7] tile counters
     ExecConfig exec_;
@@ -222,6 +252,8 @@ private:
     bool scan_withhold_ = false;
     bool prefix_valid_ = false;        // the next substep's prefix has run (for a state read)
     bool eager_prefix_ = false;        // that prefix was launched by step() behind suffix_ev_
+    bool ahead_enabled_ = true;        // set_export_ahead
+    bool ahead_ = false;               // an export ran the next substep's suffix ahead; not yet taken
     bool hashed_ = false;              // key, slot and cell counts describe the current P0 (the
                                        // last force pass hashed its output and no full prefix's scan
                                        // has consumed the counts since); else the prefix hashes

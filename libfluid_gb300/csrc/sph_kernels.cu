@@ -306,11 +306,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_single(uint32_t* __restri
     }
 }
 
-// The cell starts are invalid once a wait of the scan ran out: every pass
-// that indexes with them returns at once (the whole block alike, since no
-// pass after the scan sets that bit), and the step reports SPH_ETIMEOUT.
-__device__ __forceinline__ bool scan_failed(const uint32_t* status) {
-    return (__ldcg(status) & SPH_STATUS_SCAN_TIMEOUT) != 0u;
+// The cell starts are invalid once a wait of the scan ran out, and the cell
+// order is incomplete once the rank pass met a cell of more than
+// SPH_MAX_CELL_OCC particles (it writes no slot of that cell): every pass
+// that indexes with them returns at once, and the step reports SPH_ETIMEOUT
+// or SPH_ECELL with the particles as they were before the failed substep.
+// Each block tests once, at its start; only the rank pass raises a bit this
+// tests while later passes could see it, and its output is dropped anyway.
+__device__ __forceinline__ bool step_failed(const uint32_t* status) {
+    return (__ldcg(status) & (SPH_STATUS_SCAN_TIMEOUT | SPH_STATUS_CELL_OVERFLOW)) != 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -323,7 +327,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_scatter(const DevScene* __restrict
                                                       const uint32_t* __restrict__ slot,
                                                       uint32_t* __restrict__ tmp,
                                                       const uint32_t* __restrict__ status) {
-    if (scan_failed(status)) return;
+    if (step_failed(status)) return;
     const uint4 t = tiles[blockIdx.x];
     if (threadIdx.x >= t.z) return;
     const uint32_t i = t.y + threadIdx.x;
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
                                                           float4* __restrict__ A1,
                                                           uint32_t* __restrict__ perm,
                                                           uint32_t* __restrict__ status) {
-    if (scan_failed(status)) return;
+    if (step_failed(status)) return;
     const uint4 t = tiles[blockIdx.x];
     if (threadIdx.x >= t.z) return;
     const uint32_t g = t.y + threadIdx.x;
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                                                       uint32_t* __restrict__ tile_ctr,
                                                       const uint32_t* __restrict__ status) {
   extern __shared__ uint32_t s_rows[];
-  if (scan_failed(status)) return;
+  if (step_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
@@ -674,7 +678,7 @@ __global__ void __launch_bounds__(SPH_TILE) k_normals(const DevParams* __restric
                                                       float4* __restrict__ N, uint32_t ntiles,
                                                       uint32_t* __restrict__ tile_ctr,
                                                       const uint32_t* __restrict__ status) {
-  if (scan_failed(status)) return;
+  if (step_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     const DevParams& pp = params[t.x];
     if (!(pp.flags & 1u)) return;
@@ -766,7 +770,7 @@ k_force_integrate(const DevParams* __restrict__ params,
                                                               uint32_t* __restrict__ slot, uint32_t* __restrict__ status,
                                                               float4* __restrict__ dbg_forces, uint32_t ntiles,
                                                               uint32_t* __restrict__ tile_ctr) {
-  if (scan_failed(status)) return;
+  if (step_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     // lanes holding a particle of this tile (taken before any divergence)
     const unsigned lanes = __ballot_sync(0xffffffffu, threadIdx.x < t.z);
@@ -988,7 +992,7 @@ __global__ void k_xsph(const DevParams* __restrict__ params,
                                                    uint32_t* __restrict__ pend, uint32_t ntiles,
                                                    uint32_t* __restrict__ tile_ctr,
                                                    const uint32_t* __restrict__ status) {
-  if (scan_failed(status)) return;
+  if (step_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
     if (threadIdx.x >= t.z) return;
     const uint32_t k = t.y + threadIdx.x;
@@ -1037,12 +1041,20 @@ __global__ void __launch_bounds__(SPH_TILE) k_unsort_vel(const uint4* __restrict
                                                          const uint32_t* __restrict__ perm,
                                                          const float4* __restrict__ Vc, uint32_t base,
                                                          float* __restrict__ out, float4* __restrict__ V0,
-                                                         uint32_t* __restrict__ pend) {
+                                                         uint32_t* __restrict__ pend,
+                                                         const uint32_t* __restrict__ status,
+                                                         uint32_t* __restrict__ gate, uint32_t n) {
     const uint4 t = tiles[blockIdx.x];
+    // the status word of a force pass run ahead (launch_unsort_vel): it
+    // starts failed, so that pass does nothing, when the prefix reported an error
+    if (gate && blockIdx.x == 0 && threadIdx.x == 0) *gate = __ldcg(status) != 0u ? SPH_STATUS_SCAN_TIMEOUT : 0u;
+    // a failed prefix leaves perm incomplete (the host reports its error)
+    if (step_failed(status)) return;
     if (pend && blockIdx.x == 0 && threadIdx.x == 0) pend[t.x] = 0u;
     if (threadIdx.x >= t.z) return;
     const uint32_t f = t.y + threadIdx.x;
     const uint32_t i = __ldg(perm + f);
+    if (i - base >= n) return;   // every slot of the scene, once, after a complete prefix
     const float4 v = Vc[f];
     if (out) {
         const size_t o = 3 * (size_t)(i - base);
@@ -1051,6 +1063,31 @@ __global__ void __launch_bounds__(SPH_TILE) k_unsort_vel(const uint4* __restrict
         out[o + 2] = v.z;
     }
     if (V0) V0[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Undo a force pass run ahead of the step that takes it: the state before it
+// is what the prefix gathered (P1, A1; V1 holds the post-integration
+// velocities of a scene whose XSPH update is pending, with its previous cells
+// in the w lane), scattered back to the slots it came from.  The force pass
+// writes no array the prefix wrote, so the prefix stays valid.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(SPH_TILE) k_undo_ahead(const uint4* __restrict__ tiles,
+                                                         const uint32_t* __restrict__ perm,
+                                                         const float4* __restrict__ P1,
+                                                         const float4* __restrict__ V1,
+                                                         const float4* __restrict__ A1, float4* __restrict__ P0,
+                                                         float4* __restrict__ V2, float4* __restrict__ A0,
+                                                         uint32_t* __restrict__ okey) {
+    const uint4 t = tiles[blockIdx.x];
+    if (threadIdx.x >= t.z) return;
+    const uint32_t f = t.y + threadIdx.x;
+    const uint32_t i = __ldg(perm + f);
+    const float4 v = V1[f];
+    P0[i] = P1[f];
+    V2[i] = make_float4(v.x, v.y, v.z, 0.f);
+    A0[i] = A1[f];
+    okey[i] = __float_as_uint(v.w);
 }
 
 // ---------------------------------------------------------------------------
@@ -1237,11 +1274,17 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
                                             a.V1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0), a.status);
     return cudaGetLastError();
 }
-cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,
-                              float4* V0, bool clear_pending, cudaStream_t st) {
+cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, uint32_t n,
+                              float* out, float4* V0, bool clear_pending, cudaStream_t st, uint32_t* gate) {
     if (ntiles == 0) return cudaSuccess;
     k_unsort_vel<<<ntiles, a.block, 0, st>>>(a.tiles + first_tile, a.perm, a.Vc, base, out, V0,
-                                             clear_pending ? a.pend : nullptr);
+                                             clear_pending ? a.pend : nullptr, a.status, gate, n);
+    return cudaGetLastError();
+}
+cudaError_t launch_undo_ahead(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, cudaStream_t st) {
+    if (ntiles == 0) return cudaSuccess;
+    k_undo_ahead<<<ntiles, a.block, 0, st>>>(a.tiles + first_tile, a.perm, a.P1, a.V1, a.A1, a.P0, a.V2, a.A0,
+                                             a.okey);
     return cudaGetLastError();
 }
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st) {

@@ -71,11 +71,17 @@ cudaError_t launch_density(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st);
-// Vc (cell order, over tiles [first_tile, first_tile + ntiles) of one scene)
-// back into state order: packed xyz into `out` (particle slot - base) and/or
-// into V0; optionally clears the scene's pending flag.
-cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, float* out,
-                              float4* V0, bool clear_pending, cudaStream_t st);
+// Vc (cell order, over tiles [first_tile, first_tile + ntiles) of one scene
+// of n particles) back into state order: packed xyz into `out` (particle
+// slot - base) and/or into V0; optionally clears the scene's pending flag.
+// Does nothing after a failed prefix.  With `gate`, also
+// sets that word up as the status word of a force pass run ahead: failed (the
+// pass does nothing) when a.status reports an error.
+cudaError_t launch_unsort_vel(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, uint32_t base, uint32_t n,
+                              float* out, float4* V0, bool clear_pending, cudaStream_t st, uint32_t* gate = nullptr);
+// Undo a force pass run ahead (one scene whose XSPH update was pending, over
+// its tiles): P0, V2, A0 and okey back from the prefix's gathered copies.
+cudaError_t launch_undo_ahead(const StepArgs& a, uint32_t first_tile, uint32_t ntiles, cudaStream_t st);
 
 cudaError_t launch_unpack(const float* pos, const float* vel, uint32_t n, uint32_t base, float4* P0, float4* V0,
                           float4* A0, float4* S, cudaStream_t st);
