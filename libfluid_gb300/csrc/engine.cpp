@@ -853,6 +853,9 @@ int Engine::set_profiling(bool on) {
 int Engine::timer_mark(int slot) {
     if (slot < 0 || slot >= 64) return fail(ENG_EINVAL, "timer slot out of range");
     cudaSetDevice(device_);
+    // a region timed from here holds whole substeps: passes an export ran
+    // ahead are undone (and run again inside the region)
+    if (const int rc = settle()) return rc;
     if (!timers_[slot]) ENG_CK(cudaEventCreate(&timers_[slot]), "timer create");
     ENG_CK(cudaEventRecord(timers_[slot], stream_), "timer record");
     return ENG_OK;

@@ -175,7 +175,9 @@ private:
     int launch_suffix(bool profile);   // normals, force + integrator, [XSPH]
     int launch_suffix_args(const StepArgs& a, bool profile);
     // Undo the passes an export ran ahead, if any (see set_export_ahead):
-    // every entry point but step() and sync() calls this first.
+    // every entry point that reads or changes the state, changes how it is
+    // stepped, or marks a timer calls this first; step() takes the passes
+    // instead, and sync() only waits for them.
     int settle();
     int ensure_prefix(bool wait = true);   // the next substep's prefix, computed once
     int materialize(Scene& s);         // apply a pending XSPH update to the state
