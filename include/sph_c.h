@@ -299,7 +299,9 @@ int sph_batch_set_state(sph_batch* b, int scene_id, const float* pos, const floa
 /* Fill particles [first, first + nx*ny*nz) of a scene with a jittered
  * lattice block generated on the device. */
 int sph_batch_generate_lattice(sph_batch* b, int scene_id, const sph_lattice* spec, uint32_t first);
-/* Advance every live scene by `substeps` substeps of its own dt (blocking). */
+/* Advance every live scene by `substeps` substeps of its own dt (blocking).
+ * substeps == 0 only prepares the next step (scene layout, parameters and
+ * CUDA graphs after scenes joined or left) and launches nothing. */
 int sph_batch_step(sph_batch* b, uint32_t substeps);
 int sph_batch_step_async(sph_batch* b, uint32_t substeps);
 int sph_batch_sync(sph_batch* b);

@@ -668,12 +668,18 @@ int Engine::prepare_work() {
 int Engine::step(uint32_t substeps, bool sync) {
     cudaSetDevice(device_);
     if (scenes_.empty()) return ENG_OK;
+    // no substeps: bring the layout, parameters and graphs up to date only
+    // (a caller can then time substeps without the host work of a change)
+    if (substeps == 0) {
+        if (layout_dirty_ || params_dirty_) prefix_valid_ = false;
+        return prepare();
+    }
     // The passes an export ran ahead are this step's first substep when the
     // layout and parameters are those they ran with; their status word joins
     // this step's (the export found it clear).
     bool taken = false;
     if (ahead_) {
-        if (substeps > 0 && !layout_dirty_ && !params_dirty_ && prefix_valid_) {
+        if (!layout_dirty_ && !params_dirty_ && prefix_valid_) {
             ahead_ = false;
             taken = true;
             ENG_CK(cudaMemcpyAsync(status_, gate_, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream_),

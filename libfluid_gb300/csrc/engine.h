@@ -80,6 +80,8 @@ public:
     int load_state(int id, const float4* host, uint32_t n);
 
     // Advance every live scene by `substeps` substeps (all with their own dt).
+    // With substeps == 0, only bring the layout, parameters and captured
+    // graphs up to date (nothing is launched).
     int step(uint32_t substeps, bool sync = true);
     int sync();
 
