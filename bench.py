@@ -315,7 +315,7 @@ def run_ours(args, dist):
     L = _capi.lib()
     if args.variant is not None or args.tile is not None or args.persistent is not None:
         fs.setExec(tile=args.tile or 128, persistent=args.persistent or 0,
-                   variant=31 if args.variant is None else args.variant)
+                   variant=63 if args.variant is None else args.variant)
 
     # ---- warm-up ----
     for _ in range(args.warmup):

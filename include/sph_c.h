@@ -221,13 +221,18 @@ int sph_debug_scan_fault(sph_system* s, uint32_t spin_limit, int withhold_first_
  * blocks per SM taking tiles from a counter in the neighbour passes; skin:
  * neighbour-mask skin in units of h, in (0, 1]; variant: SPH_VARIANT_* bits
  * choosing how the neighbour walks are scheduled.  Defaults: tile 128,
- * persistent 0, skin 0.1, variant 31 (per-row density and XSPH walks,
- * 64-register force build; force and normal passes walk a row table). */
+ * persistent 0, skin 0.1, variant 63 (per-row density and XSPH walks,
+ * 64-register force build; force and normal passes walk a row table; the
+ * density scan split over three threads per particle in launches of at most
+ * 49,152 particles). */
 #define SPH_VARIANT_DENSITY_ROWS   0x1u  /* density: one loop per cell row */
 #define SPH_VARIANT_XSPH_ROWS      0x2u  /* XSPH: one loop per cell row */
 #define SPH_VARIANT_FORCE_OCC      0x4u  /* force: 64-register build, more resident warps */
 #define SPH_VARIANT_FORCE_TABLE    0x8u  /* force: row table in shared memory */
 #define SPH_VARIANT_NORMALS_TABLE  0x10u /* normals: row table in shared memory */
+#define SPH_VARIANT_DENSITY_SPLIT  0x20u /* density: three threads per particle share the candidate
+                                            scan (with DENSITY_ROWS, one block per tile, no skin
+                                            words; launches of at most 49,152 particles) */
 typedef struct sph_exec_config {
     uint32_t tile;
     uint32_t persistent;

@@ -222,7 +222,7 @@ class FluidSystem:
         (default on; results are identical either way)."""
         self._ck(self._L.sph_set_export_ahead(self._h, 1 if on else 0))
 
-    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 31) -> None:
+    def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 63) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_set_exec(self._h, C.byref(e)))

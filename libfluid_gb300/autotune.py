@@ -6,7 +6,9 @@ it): particles per tile (= threads per block), persistent blocks per SM for
 the neighbour passes (0 = one block per tile), the neighbour-mask skin, and
 then, on the best of those, the kernel-variant bits (per-row density and XSPH
 walks, the force kernel's register budget, row-table walks of the force and
-normal passes).  Each candidate is timed with CUDA events over graph-replayed
+normal passes, and for launches small enough to take it the density scan
+split over three threads per particle, which sets how many particles a warp
+scans: 32, or about 10).  Each candidate is timed with CUDA events over graph-replayed
 substeps after warm-up.  The best configuration per workload is written to
 tuned.json next to this file; the engine's compiled-in defaults (ExecConfig
 in csrc/engine.h) follow that record.
@@ -28,7 +30,11 @@ TUNED = os.path.join(HERE, "tuned.json")
 TILES = (128, 256)
 PERSISTENT = (0, 2, 4)
 SKINS = (0.1, 0.15, 0.2, 0.3)
-VARIANTS = tuple(range(32))
+VARIANTS = tuple(range(64))
+# Launches of at most this many particles take the split density scan
+# (SPH_VARIANT_DENSITY_SPLIT, bit 0x20; SPH_DENSITY_SPLIT_MAX in
+# csrc/sph_types.h); above it the bit changes nothing and is not swept.
+DENSITY_SPLIT_MAX = 49152
 
 
 def load(workload: str) -> dict | None:
@@ -81,7 +87,8 @@ def tune(workload: str, steps: int = 20, device: int = 0, variants_only: bool = 
         trials.append({"tile": tile, "persistent": pers, "skin": skin, "variant": 0, "ms_per_step": ms,
                        "particle_steps_per_s": n / (ms * 1e-3)})
     best = min(trials, key=lambda t: t["ms_per_step"])
-    for v in VARIANTS[1:]:
+    split = n <= DENSITY_SPLIT_MAX and best["persistent"] == 0
+    for v in (VARIANTS if split else VARIANTS[:32])[1:]:
         ms = time_config(scenes, best["tile"], best["persistent"], best["skin"], steps, device=device, variant=v)
         trials.append({"tile": best["tile"], "persistent": best["persistent"], "skin": best["skin"], "variant": v,
                        "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3)})

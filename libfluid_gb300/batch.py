@@ -154,7 +154,7 @@ class Batch:
     def set_use_graph(self, on: bool) -> None:
         self._ck(self._L.sph_batch_set_use_graph(self._h, 1 if on else 0))
 
-    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 31) -> None:
+    def set_exec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 63) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)
         self._ck(self._L.sph_batch_set_exec(self._h, C.byref(e)))

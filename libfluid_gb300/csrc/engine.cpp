@@ -510,6 +510,7 @@ StepArgs Engine::args() const {
     a.scenes = d_scenes_;
     a.tiles = d_tiles_;
     a.ntiles = ntiles_;
+    a.particles = (uint32_t)total_particles();
     a.total_cells = total_cells_;
     a.P0 = P0_; a.V0 = V0_; a.A0 = A0_;
     a.P1 = P1_; a.V1 = V1_; a.A1 = A1_;
@@ -792,6 +793,7 @@ int Engine::prefix_scene(const Scene& sc, bool wait) {
     StepArgs a = args();
     a.tiles = d_tiles_ + sc.tile_first;
     a.ntiles = sc.tile_count;
+    a.particles = sc.n;
     a.grid_nbr = sc.tile_count;
     a.tile_ctr = nullptr;
     a.scan_zeroes_counts = 0u;   // keep the counts for the full prefix that follows

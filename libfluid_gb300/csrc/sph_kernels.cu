@@ -435,8 +435,15 @@ __device__ __forceinline__ void ld_pos_pair(const float4* p, float4& a, float4& 
 #ifndef DENSITY_MINB
 #define DENSITY_MINB 4
 #endif
-template <int WALK, bool SKIN>
-__global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevParams* __restrict__ params,
+// SPLIT (with WALK == 1, no SKIN, one block per tile): three threads per
+// particle share phase 1, thread q of the particle taking rows 3q..3q+2; its
+// words and row-table entries are per row, so phase 1 writes exactly what
+// one thread would.  After a barrier the first thread runs phase 2 over the
+// whole table.  A small scene's pass lasts as long as one thread's walk, and
+// the split shortens the candidate scan's share of it threefold.
+template <int WALK, bool SKIN, bool SPLIT = false>
+__global__ void __launch_bounds__(SPLIT ? 3 * SPH_TILE : SPH_TILE, SPLIT ? 1 : DENSITY_MINB)
+k_density(const DevParams* __restrict__ params,
                                                       const DevScene* __restrict__ scenes,
                                                       const uint4* __restrict__ tiles,
                                                       const uint32_t* __restrict__ start,
@@ -447,28 +454,43 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
                                                       uint32_t* __restrict__ nbr_out, uint32_t ntiles,
                                                       uint32_t* __restrict__ tile_ctr,
                                                       const uint32_t* __restrict__ status) {
+  static_assert(!SPLIT || (WALK == 1 && !SKIN), "the split scan is the per-row scan without skin words");
   extern __shared__ uint32_t s_rows[];
   if (step_failed(status)) return;
   for_each_tile(tiles, ntiles, tile_ctr, [&](const uint4 t) {
-    if (threadIdx.x >= t.z) return;
-    const uint32_t k = t.y + threadIdx.x;
+    // particle li of the tile; with SPLIT, part q of its phase 1.  Every
+    // thread of a split block reaches the barrier after phase 1.
+    const uint32_t ts = SPLIT ? blockDim.x / 3u : blockDim.x;
+    const uint32_t part = SPLIT ? threadIdx.x / ts : 0u;
+    const uint32_t li = SPLIT ? threadIdx.x - part * ts : threadIdx.x;
+    if (!SPLIT && li >= t.z) return;
+    const bool act = !SPLIT || li < t.z;
+    const uint32_t k = t.y + li;
     const DevScene sc = scenes[t.x];
     const DevParams& pp = params[t.x];
-    const float4 p = P1[k];
-    const float4 vi = V1[k];
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f), vi = p;
+    if (act) {
+        p = P1[k];
+        vi = V1[k];
+    }
     const int3 g = grid_of(pp, p.x, p.y, p.z);
-    if (!grid_inside(pp, g)) {
-        S[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        Vc[k] = make_float4(vi.x, vi.y, vi.z, 0.f);
-        if (nbr_out) nbr_out[k] = 0;
-        return;
+    const bool work = act && grid_inside(pp, g);
+    if (act && !work) {
+        if (part == 0u) {
+            S[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            Vc[k] = make_float4(vi.x, vi.y, vi.z, 0.f);
+            if (nbr_out) nbr_out[k] = 0;
+        }
+        if (!SPLIT) return;
     }
     const uint32_t delta = sc.part_base - __ldg(start + sc.cell_base);
     // the skin-radius words serve only the per-substep XSPH pass
     const float h2 = pp.h2, skin2 = SKIN ? pp.skin2 : pp.h2, eps = pp.eps;
-    uint32_t* tab = s_rows + threadIdx.x;
-    const uint32_t ts = blockDim.x;
+    uint32_t* tab = s_rows + li;
     uint32_t live = 0u, full = 0u;
+    // rows of this thread's phase 1
+    constexpr int kRows = SPLIT ? 3 : 9;
+    const int r0 = SPLIT ? 3 * (int)part : 0;
 
     // ---- phase 1: distance test of every candidate ----
     auto visit = [&](const float4& q, uint32_t bit, uint32_t& dm, uint32_t& sm) {
@@ -515,9 +537,10 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     // the row replaces it.
     uint32_t rows = 0u;
 #pragma unroll
-    for (int r = 0; r < 9; ++r) {
+    for (int rr = 0; rr < kRows; ++rr) {
+        const int r = r0 + rr;
         uint32_t jb0, je0;
-        if (row_range(pp, start, sc.cell_base, delta, g, r, jb0, je0)) {
+        if ((!SPLIT || work) && row_range(pp, start, sc.cell_base, delta, g, r, jb0, je0)) {
             rows |= 1u << r;
             tab[r * ts] = jb0;
             tab[(9 + 2 * r) * ts] = je0;
@@ -525,7 +548,8 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
     }
     if (WALK == 1) {
 #pragma unroll 1
-        for (int r = 0; r < 9; ++r) {
+        for (int rr = 0; rr < kRows; ++rr) {
+            const int r = r0 + rr;
             if (!((rows >> r) & 1u)) continue;
             const uint32_t jb0 = tab[r * ts], je0 = tab[(9 + 2 * r) * ts];
             const uint32_t len = je0 - jb0;
@@ -603,6 +627,17 @@ __global__ void __launch_bounds__(SPH_TILE, DENSITY_MINB) k_density(const DevPar
             bit <<= 1;
             ++j;
         }
+    }
+
+    if constexpr (SPLIT) {
+        // the parts' row bits are disjoint: the first thread takes their union
+        __shared__ uint32_t s_bits[2 * 3 * SPH_TILE];
+        s_bits[2 * threadIdx.x] = live;
+        s_bits[2 * threadIdx.x + 1] = full;
+        __syncthreads();
+        if (part != 0u || !work) return;
+        live = s_bits[2 * li] | s_bits[2 * (ts + li)] | s_bits[2 * (2 * ts + li)];
+        full = s_bits[2 * li + 1] | s_bits[2 * (ts + li) + 1] | s_bits[2 * (2 * ts + li) + 1];
     }
 
     // ---- phase 2: the density pairs, in candidate order ----
@@ -1216,7 +1251,8 @@ cudaError_t init_kernel_attributes() {
         (const void*)k_force_integrate<false, 3, true>, (const void*)k_force_integrate<false, 4, true>,
         (const void*)k_normals<true>,
         (const void*)k_density<0, false>, (const void*)k_density<0, true>,
-        (const void*)k_density<1, false>, (const void*)k_density<1, true>};
+        (const void*)k_density<1, false>, (const void*)k_density<1, true>,
+        (const void*)k_density<1, false, true>};
     for (const void* f : fns) {
         const cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
         if (e != cudaSuccess) return e;
@@ -1265,11 +1301,21 @@ cudaError_t launch_sort(const StepArgs& a, cudaStream_t st) {
                                                 a.okey, a.pend, a.P1, a.V1, a.A1, a.perm, a.status);
     return cudaGetLastError();
 }
+bool density_split(const StepArgs& a) {
+    return (a.variant & SPH_VARIANT_DENSITY_SPLIT) != 0u && (a.variant & SPH_VARIANT_DENSITY_ROWS) != 0u &&
+           !a.skin_masks && a.tile_ctr == nullptr && a.particles <= SPH_DENSITY_SPLIT_MAX;
+}
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st) {
+    const size_t smem = (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t);   // the row table
+    if (density_split(a)) {
+        k_density<1, false, true><<<a.ntiles, 3u * a.block, smem, st>>>(
+            a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride, a.V1, a.pend, a.Vc, a.dbg_nbr,
+            a.ntiles, nullptr, a.status);
+        return cudaGetLastError();
+    }
     const bool rows = (a.variant & SPH_VARIANT_DENSITY_ROWS) != 0u;
     auto kern = a.skin_masks ? (rows ? k_density<1, true> : k_density<0, true>)
                              : (rows ? k_density<1, false> : k_density<0, false>);
-    const size_t smem = (size_t)SPH_ROW_TABLE_WORDS * a.block * sizeof(uint32_t);   // the row table
     kern<<<a.grid_nbr, a.block, smem, st>>>(a.params, a.scenes, a.tiles, a.start, a.P1, a.S, a.mask, a.mask_stride,
                                             a.V1, a.pend, a.Vc, a.dbg_nbr, a.ntiles, ctr(a, 0), a.status);
     return cudaGetLastError();

@@ -12,6 +12,7 @@ struct StepArgs {
     const DevScene* scenes;
     const uint4* tiles;        // (scene, first slot, count, 0)
     uint32_t ntiles;
+    uint32_t particles;        // particles the tiles hold
     uint32_t total_cells;      // packed cell arena size including NULL buckets
     float4 *P0, *V0, *A0;      // state
     float4 *P1, *V1, *A1;      // cell-ordered state
@@ -68,6 +69,10 @@ cudaError_t launch_scan_raw(const uint32_t* counts, uint32_t n, uint32_t* tile_s
                             cudaStream_t st);
 cudaError_t launch_sort(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_density(const StepArgs& a, cudaStream_t st);
+// Whether launch_density splits the candidate scan (SPH_VARIANT_DENSITY_SPLIT:
+// the per-row scan without skin words, one block per tile, and at most
+// SPH_DENSITY_SPLIT_MAX particles in the launch).
+bool density_split(const StepArgs& a);
 cudaError_t launch_normals(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_force(const StepArgs& a, cudaStream_t st);
 cudaError_t launch_xsph(const StepArgs& a, cudaStream_t st);

@@ -71,9 +71,18 @@ struct DevParams {
 #define SPH_VARIANT_FORCE_OCC     0x4u   // force: 64-register build (more resident warps)
 #define SPH_VARIANT_FORCE_TABLE   0x8u   // force: walk over a per-thread row table in shared memory
 #define SPH_VARIANT_NORMALS_TABLE 0x10u  // normals: the same
-#define SPH_VARIANT_MASK          0x1fu
-#define SPH_VARIANT_DEFAULT       0x1fu  // measured fastest on the 1M dam break, the 256-scene batch
-                                         // and the 8M tension scene
+#define SPH_VARIANT_DENSITY_SPLIT 0x20u  // density: three threads per particle share the candidate scan
+                                         // (launches of at most SPH_DENSITY_SPLIT_MAX particles)
+#define SPH_VARIANT_MASK          0x3fu
+#define SPH_VARIANT_DEFAULT       0x3fu  // measured fastest on the 1M dam break, the 256-scene batch
+                                         // and the 8M tension scene (where the split scan does not
+                                         // apply), and on dam breaks of 8,000 to 32,768 particles
+// Largest launch (particles over all tiles) that the split scan serves: it
+// gained 6-9% per substep on dam breaks of 8,000 to 32,768 particles and lost
+// 10% at 64,000 (the blocks of three times the threads run fewer at once).
+#ifndef SPH_DENSITY_SPLIT_MAX
+#define SPH_DENSITY_SPLIT_MAX     49152u
+#endif
 
 // Scene placement in the engine's arenas.
 struct DevScene {

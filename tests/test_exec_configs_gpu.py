@@ -34,11 +34,26 @@ def test_configs_bit_identical(exe):
         assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 4, 7, 8, 12, 15, 16, 31])
+@pytest.mark.parametrize("tile", [64, 128, 256])
+def test_split_scan_bit_identical(tile):
+    """The density scan split over three threads per particle (launches of
+    at most 49,152 particles; this one holds 40,928), at every tile size,
+    against the one-thread scan, with surface tension in one scene."""
+    specs = [W.small_dam_break(seed=12)] + W.batch_manifest(num_scenes=1, seed=43, nmin=8000, nmax=8000)
+    assert sum(s.n for s in specs) <= 49152
+    base = _run(specs, 6, tile=tile, persistent=0, skin=0.1, variant=31)
+    other = _run(specs, 6, tile=tile, persistent=0, skin=0.1, variant=63)
+    for (pa, ca, va), (pb, cb, vb) in zip(base, other):
+        assert np.array_equal(pa, pb) and np.array_equal(va, vb) and np.array_equal(ca, cb)
+
+
+@pytest.mark.parametrize("variant", [1, 2, 4, 7, 8, 12, 15, 16, 31, 33, 63])
 def test_variants_bit_identical(variant):
-    """Per-row density/XSPH walks, the 64-register force kernel and the
-    force kernel's row-table walk visit neighbours in the same order as the
-    default walks: identical results, with and without surface tension."""
+    """Per-row density/XSPH walks, the density scan split over three
+    threads per particle (in the single-scene runs below), the 64-register
+    force kernel and the force kernel's row-table walk visit neighbours in
+    the same order as the default walks: identical results, with and without
+    surface tension."""
     specs = W.batch_manifest(num_scenes=3, seed=37, nmin=2000, nmax=9000)
     specs.append(W.small_dam_break(seed=10))
     base = _run(specs, 6, tile=128, persistent=0, skin=0.1, variant=0)
@@ -59,7 +74,7 @@ def test_eager_equals_graph():
 
 
 @pytest.mark.parametrize("deferred", [True, False])
-@pytest.mark.parametrize("variant", [1, 2, 8, 16, 31])
+@pytest.mark.parametrize("variant", [1, 2, 8, 16, 31, 33, 63])
 def test_variants_bit_identical_crowded(variant, deferred):
     """The same on compressed lattices whose cell rows hold 33 to 160
     candidates, so the two-word masks and the rows walked in full meet every
