@@ -503,11 +503,15 @@ def measure_batched(dist, num_scenes: int, steps: int, warmup: int, clocks_csv=N
     value = total_n * steps / (ms * 1e-3)
     b.close()
     # the plain step, one scene at a time: each scene in its own engine, the
-    # same warm-up, then the same substeps timed (graph replay)
+    # same warm-up, then the same substeps timed (graph replay).  A scene
+    # alone is small enough for the split density scan (variant bit 0x20),
+    # which the batch's own launches are too large to take.
+    plain_exe = dict(exe)
+    plain_exe["variant"] = exe.get("variant", 63) | 0x20
     plain_ms = 0.0
     for s in specs:
         one = Batch(dist.local)
-        one.set_exec(**exe)
+        one.set_exec(**plain_exe)
         one.add_scene(s)
         for _ in range(warmup):
             one.step(1)
@@ -524,7 +528,7 @@ def measure_batched(dist, num_scenes: int, steps: int, warmup: int, clocks_csv=N
             "workload": f"{len(specs)} {BATCH_DESC}",
             "timing": "CUDA events, graph replay, one launch per pass",
             "exec": exe or "engine defaults",
-            "plain_one_at_a_time": {"value": plain, "steps": steps, "warmup": warmup,
+            "plain_one_at_a_time": {"value": plain, "steps": steps, "warmup": warmup, "exec": plain_exe,
                                     "how": "each scene alone in its own engine, the same warm-up and the same "
                                            "substeps, graph replay, summed device time"},
             "speedup_vs_plain": value / plain, "clocks": clk}
