@@ -222,6 +222,12 @@ class FluidSystem:
         (default on; results are identical either way)."""
         self._ck(self._L.sph_set_export_ahead(self._h, 1 if on else 0))
 
+    def exportAheadStats(self) -> dict:
+        """Exports that ran passes ahead, and how many were taken or undone."""
+        out = (C.c_uint64 * 3)()
+        self._ck(self._L.sph_export_ahead_stats(self._h, out))
+        return {"started": out[0], "taken": out[1], "undone": out[2]}
+
     def setExec(self, tile: int = 128, persistent: int = 0, skin: float = 0.1, variant: int = 63) -> None:
         from ._capi import SphExec
         e = SphExec(tile, persistent, skin, variant)

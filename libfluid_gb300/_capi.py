@@ -102,6 +102,7 @@ SIGNATURES = [
     ("sph_debug_get", _I, [_P, _I, _P, C.c_uint64]),
     ("sph_set_use_graph", _I, [_P, _I]),
     ("sph_set_export_ahead", _I, [_P, _I]),
+    ("sph_export_ahead_stats", _I, [_P, C.POINTER(C.c_uint64)]),
     ("sph_set_profiling", _I, [_P, _I]),
     ("sph_set_exec", _I, [_P, C.POINTER(SphExec)]),
     ("sph_set_deferred_xsph", _I, [_P, _I]),

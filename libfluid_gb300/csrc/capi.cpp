@@ -427,6 +427,11 @@ int sph_set_export_ahead(sph_system* s, int on) {
     if (!s) return SPH_EINVAL;
     return eng_err(s, s->eng->set_export_ahead(on != 0));
 }
+int sph_export_ahead_stats(const sph_system* s, uint64_t* out) {
+    if (!s || !out || !s->eng) return SPH_EINVAL;
+    s->eng->export_ahead_stats(out);
+    return SPH_OK;
+}
 int sph_set_deferred_xsph(sph_system* s, int on) {
     if (!s) return SPH_EINVAL;
     return eng_err(s, s->eng->set_deferred_xsph(on != 0));

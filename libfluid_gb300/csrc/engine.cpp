@@ -609,6 +609,11 @@ int Engine::read_status() {
 int Engine::settle() {
     if (!ahead_) return ENG_OK;
     ahead_ = false;
+    ++ahead_undone_;
+    if (++ahead_misses_ >= 2u) {
+        ahead_skip_ = 16u;
+        ahead_misses_ = 1u;   // one more miss after the pause pauses again
+    }
     cudaSetDevice(device_);
     const Scene& s = scenes_.front();
     ENG_CK(launch_undo_ahead(args(), s.tile_first, s.tile_count, stream_), "undo");
@@ -682,6 +687,8 @@ int Engine::step(uint32_t substeps, bool sync) {
     if (ahead_) {
         if (!layout_dirty_ && !params_dirty_ && prefix_valid_) {
             ahead_ = false;
+            ahead_misses_ = 0u;
+            ++ahead_taken_;
             taken = true;
             ENG_CK(cudaMemcpyAsync(status_, gate_, sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream_),
                    "status merge");
@@ -1005,8 +1012,12 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
         // normal and force passes, with their own status word, which starts
         // failed when the prefix reported an error; they write the state
         // only after the pack has read it.
-        const bool ahead = pend && ahead_enabled_ && all_defer_ && use_graph_ && !profiling_ && !debug_ &&
-                           scenes_.size() == 1;
+        bool ahead = pend && ahead_enabled_ && all_defer_ && use_graph_ && !profiling_ && !debug_ &&
+                     scenes_.size() == 1;
+        if (ahead && ahead_skip_ > 0) {
+            --ahead_skip_;
+            ahead = false;
+        }
         ENG_CK(cudaStreamWaitEvent(copy_stream_, suffix_ev_, 0), "export wait");
         ENG_CK(launch_pack(P0_, V0_, n, s->part_base, s->dp.inv_rest_density, dp, dc, pend ? nullptr : dv,
                            copy_stream_), "pack");
@@ -1031,6 +1042,7 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
                 rc = launch_suffix_args(b, false);
                 if (rc) return rc;
                 ahead_ = true;
+                ++ahead_started_;
             } else {
                 ENG_CK(cudaMemcpyAsync(vel, dv, bytes, cudaMemcpyDeviceToHost, stream_), "download");
             }

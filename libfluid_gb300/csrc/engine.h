@@ -134,6 +134,13 @@ public:
         return rc;
     }
     bool export_ahead() const { return ahead_enabled_; }
+    // Exports that ran passes ahead, and how many of those a step took and
+    // how many were undone.
+    void export_ahead_stats(uint64_t out[3]) const {
+        out[0] = ahead_started_;
+        out[1] = ahead_taken_;
+        out[2] = ahead_undone_;
+    }
     int set_exec(const ExecConfig& e);
     const ExecConfig& exec() const { return exec_; }
     int sm_count() const { return sm_count_; }
@@ -258,6 +265,12 @@ private:
     bool eager_prefix_ = false;        // that prefix was launched by step() behind suffix_ev_
     bool ahead_enabled_ = true;        // set_export_ahead
     bool ahead_ = false;               // an export ran the next substep's suffix ahead; not yet taken
+    // A caller whose next call rarely takes the passes (a time step that
+    // changes every frame, reads after the export) would pay for them: after
+    // two undone in a row the next 16 exports run nothing ahead, then one
+    // tries again.
+    uint32_t ahead_misses_ = 0, ahead_skip_ = 0;
+    uint64_t ahead_started_ = 0, ahead_taken_ = 0, ahead_undone_ = 0;
     bool hashed_ = false;              // key, slot and cell counts describe the current P0 (the
                                        // last force pass hashed its output and no full prefix's scan
                                        // has consumed the counts since); else the prefix hashes

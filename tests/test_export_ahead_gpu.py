@@ -53,37 +53,47 @@ def _positions_only(fs):
     return pos
 
 
-def _ops(spec, snap_box):
+def _ops(spec, snap_box, last):
+    """Calls that take the passes run ahead (advances at an unchanged time
+    step: 2 * dt over 2 substeps is dt exactly) and calls that undo them (a
+    return from half the time step to the whole one is such a call too), each
+    undoing call followed by advances that take the next ones: two undone in
+    a row would pause the option (Engine::settle)."""
     dt = spec.dt
 
     def snapshot(fs):
         snap_box[fs] = fs.snapshot()
         return snap_box[fs]
 
-    return [
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("export again", lambda fs: None),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("snapshot", snapshot),
-        ("advance x3", lambda fs: fs.advance(3 * dt, 3)),
-        ("viscosity", lambda fs: fs.setViscosity(spec.viscosity * 1.5)),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("half dt", lambda fs: fs.advance(0.5 * dt, 1)),
-        ("density tap", lambda fs: fs.debug("density")),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("async + sync", lambda fs: (fs.advanceAsync(dt, 2), fs.sync())),
-        ("sync", lambda fs: fs.sync()),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("per-substep xsph", lambda fs: (fs.setDeferredXSPH(False), fs.advance(dt, 1), fs.setDeferredXSPH(True))),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("tile 64", lambda fs: fs.setExec(**{**fs.getExec(), "tile": 64})),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("restore", lambda fs: fs.restore(snap_box[fs])),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("set state", lambda fs: fs.setState(*_export(fs)[::2])),
-        ("advance", lambda fs: fs.advance(dt, 1)),
-        ("advance", lambda fs: fs.advance(dt, 1)),
+    def adv(fs):
+        return fs.advance(dt, 1)
+
+    def half(fs):
+        return fs.advance(0.5 * dt, 1)
+
+    # each undoing call with the advance that follows it twice: the first
+    # runs passes ahead again (if the call left nothing pending), the second
+    # takes them
+    undoing = [
+        ("export again", lambda fs: None, adv),
+        ("snapshot", snapshot, adv),
+        ("viscosity", lambda fs: fs.setViscosity(spec.viscosity * 1.5), adv),
+        ("half dt", half, half),
+        ("whole dt", adv, adv),   # back from half the time step: undoes those run with it
+        ("density tap", lambda fs: fs.debug("density"), adv),
+        ("sync", lambda fs: fs.sync(), adv),   # the export after it undoes them
+        ("per-substep xsph", lambda fs: (fs.setDeferredXSPH(False), fs.advance(dt, 1), fs.setDeferredXSPH(True)),
+         adv),
+        ("tile 64", lambda fs: fs.setExec(**{**fs.getExec(), "tile": 64}), adv),
+        ("restore", lambda fs: fs.restore(snap_box[fs]), adv),
+        ("set state", lambda fs: fs.setState(last[fs][0], last[fs][2]), adv),
     ]
+    ops = [("advance", adv), ("advance x2", lambda fs: fs.advance(2 * dt, 2))]
+    for name, call, follow in undoing:
+        ops += [(name, call), ("advance", follow), ("advance", follow)]
+    # an async step takes them too; its export runs nothing ahead
+    ops += [("async + sync", lambda fs: (fs.advanceAsync(dt, 2), fs.sync())), ("advance", adv), ("advance", adv)]
+    return ops
 
 
 @pytest.mark.parametrize("case", ["dam", "tension", "persistent"])
@@ -99,17 +109,24 @@ def test_export_ahead_changes_nothing(case):
     if case == "persistent":
         kw = {"persistent": 2}
     on, off = _pair(spec, **kw)
-    snaps = {}
+    snaps, last = {}, {}
     try:
         for fs in (on, off):
             fs.advance(spec.dt, 1)
-        assert _same(_export(on), _export(off))
-        for name, op in _ops(spec, snaps):
+            last[fs] = _export(fs)
+        assert _same(last[on], last[off])
+        for name, op in _ops(spec, snaps, last):
             r_on, r_off = op(on), op(off)
             if isinstance(r_on, (bytes, np.ndarray)):
                 assert np.array_equal(np.frombuffer(r_on, np.uint8) if isinstance(r_on, bytes) else r_on,
                                       np.frombuffer(r_off, np.uint8) if isinstance(r_off, bytes) else r_off), name
-            assert _same(_export(on), _export(off)), name
+            last[on], last[off] = _export(on), _export(off)
+            assert _same(last[on], last[off]), name
+        # the passes ran ahead after most exports, and both fates were met
+        st = on.exportAheadStats()
+        print(case, st)
+        assert st["started"] >= 15 and st["taken"] >= 8 and st["undone"] >= 8
+        assert off.exportAheadStats() == {"started": 0, "taken": 0, "undone": 0}
     finally:
         on.close()   # with passes run ahead still in flight
         off.close()
@@ -125,6 +142,29 @@ def test_export_ahead_frame_loop_matches():
             on.advance(spec.dt, 1)
             off.advance(spec.dt, 1)
             assert _same(_export(on), _export(off))
+        # every export ran the next force pass ahead and each advance took it
+        assert on.exportAheadStats() == {"started": 40, "taken": 39, "undone": 0}
+    finally:
+        on.close()
+        off.close()
+
+
+def test_export_ahead_with_a_changing_time_step():
+    """A time step that changes every frame: every pass run ahead is undone,
+    so the option pauses after two and tries again after 16 exports; 60
+    frames, the same bits as without the option."""
+    spec = W.small_dam_break(seed=33)
+    on, off = _pair(spec)
+    try:
+        for f in range(60):
+            dt = spec.dt * (1.0 + 0.01 * (f % 7))
+            on.advance(dt, 1)
+            off.advance(dt, 1)
+            assert _same(_export(on), _export(off)), f
+        # two undone, a pause of 16 exports, one more try: a handful in 60 frames
+        st = on.exportAheadStats()
+        print(st)
+        assert st["taken"] == 0 and 3 <= st["started"] <= 8 and st["started"] - 1 <= st["undone"] <= st["started"]
     finally:
         on.close()
         off.close()
