@@ -8,8 +8,9 @@ inputs.  A step is one WCSPH substep of that scene (advance(dt, 1)).
   value      particle-steps/s with the state resident in HBM: K substeps
              replayed as a CUDA graph, CUDA events on the library's stream.
   roofline   dominant kernel from a per-pass CUDA-event region of the same
-             workload; algorithmic bytes per launch / mean launch time,
-             against the measured HBM copy bandwidth.
+             workload (50 substeps from the middle of the timed run, replayed
+             from its start state); algorithmic bytes per launch / mean
+             launch time, against the measured HBM copy bandwidth.
   e2e        the fluidtest frame loop through the C ABI with host buffers
              (pinned): setupFromData (H2D) then K x (advance + exportToData
              of positions, colours, velocities to the host).
@@ -321,6 +322,7 @@ def run_ours(args, dist):
     for _ in range(args.warmup):
         fs.advance(spec.dt, 1)
     fs.sync()
+    start_state = fs.snapshot()   # the per-pass region below replays the timed run from here
 
     # ---- timed region: K substeps as CUDA-graph replays, state resident ----
     clocks = ClockSampler(dist.local, args.clocks_csv)
@@ -340,7 +342,14 @@ def run_ours(args, dist):
     value = total / (ms_max * 1e-3)
 
     # ---- per-pass region: CUDA events around every pass (eager launches) ----
+    # over substeps from the middle of the timed run (the scene compresses as
+    # it runs, so its first or last substeps would misstate the average one):
+    # the timed run's start state, advanced half of its substeps, untimed
     prof_steps = max(3, min(args.steps, 50))
+    fs.restore(start_state)
+    for _ in range(max(0, args.steps // 2 - prof_steps // 2)):
+        fs.advanceAsync(spec.dt, 1)
+    fs.sync()
     fs.setProfiling(True)
     for _ in range(prof_steps):
         fs.advance(spec.dt, 1)
@@ -372,7 +381,9 @@ def run_ours(args, dist):
                 "step_alg_bytes": sum(ALG_BYTES[k] for k in ("hash", "sort", "density", "force_integrate", "xsph"))
                 * n + CELL_BYTES * cells,
                 "pass_share": {k: v / per_launch["substep"] for k, v in kern.items()},
-                "issue": profile_counters(dom, args.workload)}
+                "issue": profile_counters(dom, args.workload),
+                "window": f"{prof_steps} eager substeps from substep {args.warmup + max(0, args.steps // 2 - prof_steps // 2)} "
+                          f"of the timed run (the middle of its {args.steps}), CUDA events around every pass"}
     roofline["step_frac"] = roofline["step_alg_bytes"] / (ms_max / args.steps * 1e-3) / 1e9 / peak
 
     # ---- end to end through the C ABI with pinned host buffers ----
