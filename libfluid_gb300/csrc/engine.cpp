@@ -130,10 +130,10 @@ Engine::~Engine() {
     if (stream_) cudaStreamSynchronize(stream_);
     if (copy_stream_) cudaStreamSynchronize(copy_stream_);
     free_all();
-    if (exec_pre_) cudaGraphExecDestroy(exec_pre_);
-    if (exec_suf_) cudaGraphExecDestroy(exec_suf_);
-    if (graph_pre_) cudaGraphDestroy(graph_pre_);
-    if (graph_suf_) cudaGraphDestroy(graph_suf_);
+    for (cudaGraphExec_t e : {exec_pre_, exec_suf_, exec_full_})
+        if (e) cudaGraphExecDestroy(e);
+    for (cudaGraph_t g : {graph_pre_, graph_suf_, graph_full_})
+        if (g) cudaGraphDestroy(g);
     for (auto& e : ev_) if (e) cudaEventDestroy(e);
     for (auto& e : timers_) if (e) cudaEventDestroy(e);
     if (status_) cudaFree(status_);
@@ -627,7 +627,7 @@ int Engine::settle() {
 
 // Layout, parameters and (in graph mode) the two captured graphs up to date.
 int Engine::prepare() {
-    if (!layout_dirty_ && !params_dirty_ && !graph_dirty_ && exec_pre_ && exec_suf_) return ENG_OK;
+    if (!layout_dirty_ && !params_dirty_ && !graph_dirty_ && exec_pre_ && exec_suf_ && exec_full_) return ENG_OK;
     const auto t0 = std::chrono::steady_clock::now();
     const int rc = prepare_work();
     prep_seconds_ += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -639,15 +639,18 @@ int Engine::prepare_work() {
     if (layout_dirty_) { int rc = rebuild_layout(); if (rc) return rc; }
     if (params_dirty_) { int rc = upload_params(); if (rc) return rc; }
     const bool graph = use_graph_ && !profiling_;
-    if (graph && (graph_dirty_ || !exec_pre_ || !exec_suf_)) {
+    if (graph && (graph_dirty_ || !exec_pre_ || !exec_suf_ || !exec_full_)) {
         // Re-capture; when only launch sizes and arguments changed (scenes
         // joined or left), update the instantiated graphs in place, which is
         // much cheaper than instantiating again.
-        for (int half = 0; half < 2; ++half) {
-            cudaGraph_t& gref = half == 0 ? graph_pre_ : graph_suf_;
-            cudaGraphExec_t& eref = half == 0 ? exec_pre_ : exec_suf_;
+        cudaGraph_t* graphs[] = {&graph_pre_, &graph_suf_, &graph_full_};
+        cudaGraphExec_t* execs[] = {&exec_pre_, &exec_suf_, &exec_full_};
+        for (int part = 0; part < 3; ++part) {
+            cudaGraph_t& gref = *graphs[part];
+            cudaGraphExec_t& eref = *execs[part];
             ENG_CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "begin capture");
-            int rc = half == 0 ? launch_prefix_args(args(), false, false) : launch_suffix(false);
+            int rc = part == 1 ? ENG_OK : launch_prefix_args(args(), false, false);
+            if (rc == ENG_OK && part != 0) rc = launch_suffix(false);
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(stream_, &g);
             if (rc) { if (g) cudaGraphDestroy(g); return rc; }
@@ -707,9 +710,10 @@ int Engine::step(uint32_t substeps, bool sync) {
         } else if (graph) {
             if (!prefix_valid_) {
                 if (!hashed_) { rc = launch_hash_standalone(args()); if (rc) return rc; }
-                ENG_CK(cudaGraphLaunch(exec_pre_, stream_), "graph launch");
+                ENG_CK(cudaGraphLaunch(exec_full_, stream_), "graph launch");   // prefix and suffix
+            } else {
+                ENG_CK(cudaGraphLaunch(exec_suf_, stream_), "graph launch");
             }
-            ENG_CK(cudaGraphLaunch(exec_suf_, stream_), "graph launch");
         } else if (profiling_) {
             // a prefix computed for a state read is recomputed (same values) so
             // that every pass of the substep is timed

@@ -274,8 +274,10 @@ private:
     bool hashed_ = false;              // key, slot and cell counts describe the current P0 (the
                                        // last force pass hashed its output and no full prefix's scan
                                        // has consumed the counts since); else the prefix hashes
-    cudaGraph_t graph_pre_ = nullptr, graph_suf_ = nullptr;
-    cudaGraphExec_t exec_pre_ = nullptr, exec_suf_ = nullptr;
+    // the substep captured as prefix, suffix, and both in one graph (one
+    // launch per substep in a run of substeps)
+    cudaGraph_t graph_pre_ = nullptr, graph_suf_ = nullptr, graph_full_ = nullptr;
+    cudaGraphExec_t exec_pre_ = nullptr, exec_suf_ = nullptr, exec_full_ = nullptr;
     cudaEvent_t ev_[kPasses + 1] = {};
     cudaEvent_t timers_[64] = {};
     double pass_ms_[kPasses] = {};
