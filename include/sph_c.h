@@ -261,8 +261,9 @@ int sph_set_use_graph(sph_system* s, int on);     /* CUDA-graph replay of the su
  * Results are the same bit for bit either way. */
 int sph_set_export_ahead(sph_system* s, int on);
 /* out[0]: exports that ran passes ahead; out[1]: of those, taken by an
- * advance; out[2]: undone.  After two undone in a row the next 16 exports
- * run nothing ahead. */
+ * advance; out[2]: undone (out[0] = out[1] + out[2], plus one while passes
+ * wait to be taken).  After two undone in a row the next 16 exports run
+ * nothing ahead. */
 int sph_export_ahead_stats(const sph_system* s, uint64_t* out);
 int sph_set_profiling(sph_system* s, int on);     /* per-pass CUDA events (disables the graph) */
 /* Accumulated per-pass milliseconds since profiling was enabled, in the

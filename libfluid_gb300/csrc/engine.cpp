@@ -1056,8 +1056,9 @@ int Engine::get_state(int id, float* pos, float* colour, float* vel, uint32_t n,
         if (ahead_) {
             if (*h_status_ == 0u) return ENG_OK;
             // the passes run ahead found their status word failed and did
-            // nothing: report the prefix's error as below
+            // nothing (they do not count as run): report the prefix's error
             ahead_ = false;
+            --ahead_started_;
         }
         rc = read_status();   // the prefix's status; waits for the main stream too
         if (rc) { prefix_valid_ = false; eager_prefix_ = false; return rc; }
