@@ -225,6 +225,8 @@ def test_cell_overflow_in_the_prefix_of_an_export():
             with pytest.raises(_capi.SphError) as err:
                 fs.exportToData()
             assert err.value.code == _capi.SPH_ECELL
+            # the passes launched ahead found the prefix failed: none ran
+            assert fs.exportAheadStats()["started"] == 0
             moved[ahead] = _positions_only(fs)
             assert np.all(moved[ahead][4200:, 0] < 0.55)   # all 8,400 in the one cell
             with pytest.raises(_capi.SphError) as err:
