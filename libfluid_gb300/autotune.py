@@ -37,6 +37,15 @@ VARIANTS = tuple(range(64))
 DENSITY_SPLIT_MAX = 49152
 
 
+def variants_for(particles: int, persistent: int) -> tuple:
+    """The variant values worth timing for a launch of `particles` particles:
+    all 64 where the split density scan can apply (one block per tile and a
+    small enough launch), else the 32 without its bit, which would change
+    nothing there."""
+    split = particles <= DENSITY_SPLIT_MAX and persistent == 0
+    return VARIANTS if split else VARIANTS[:32]
+
+
 def load(workload: str) -> dict | None:
     try:
         return json.load(open(TUNED))[workload]["best"]
@@ -87,8 +96,7 @@ def tune(workload: str, steps: int = 20, device: int = 0, variants_only: bool = 
         trials.append({"tile": tile, "persistent": pers, "skin": skin, "variant": 0, "ms_per_step": ms,
                        "particle_steps_per_s": n / (ms * 1e-3)})
     best = min(trials, key=lambda t: t["ms_per_step"])
-    split = n <= DENSITY_SPLIT_MAX and best["persistent"] == 0
-    for v in (VARIANTS if split else VARIANTS[:32])[1:]:
+    for v in variants_for(n, best["persistent"])[1:]:
         ms = time_config(scenes, best["tile"], best["persistent"], best["skin"], steps, device=device, variant=v)
         trials.append({"tile": best["tile"], "persistent": best["persistent"], "skin": best["skin"], "variant": v,
                        "ms_per_step": ms, "particle_steps_per_s": n / (ms * 1e-3)})
