@@ -405,8 +405,11 @@ __global__ void __launch_bounds__(SPH_TILE) k_rank_gather(const DevScene* __rest
 // (about one candidate in six), so a warp no longer runs the neighbour path
 // on every candidate that any of its lanes accepts.  Rows longer than 64
 // candidates are not scanned in phase 1; phase 2 walks them in full with the
-// test.  Both phases visit candidates in the reference's order, so the sum is
-// the candidate-order sum.  WALK selects phase 1's loop: flattened across the
+// test.  Both phases visit candidates in the same order (rows z outer, then
+// y, then slots, the row's cells x ascending), so the sum follows phase 1's
+// candidate order; the reference's loop runs the cells x outer and z inner
+// (fluidphysics.cu:29-33), the same terms in another order.  WALK selects
+// phase 1's loop: flattened across the
 // rows (0) or one loop per row with four candidates in flight, two per
 // 256-bit load (1); the words are
 // the same.
